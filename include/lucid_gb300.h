@@ -1,0 +1,366 @@
+/*
+ * lucid_gb300 — C ABI of a GB300-native (sm_103a) replacement for LucidRaster's compute
+ * rasterization passes (quad setup → bin counter → bin categorizer → bin dispatcher →
+ * raster low/high with exact front-to-back OIT blending).
+ *
+ * Every entry point is plain C: plain pointers and sizes, no C++ or CUDA types in the
+ * signatures. Streams are passed as `void*` holding a `cudaStream_t` (NULL = legacy default
+ * stream). Geometry and output pointers are DEVICE pointers borrowed for the duration of the
+ * call; the renderer owns every scratch buffer it needs (allocated once in lucid_create).
+ *
+ * All functions return lucid_status. Device-side capacity problems are not fatal: they are
+ * recorded in lucid_info.error_code (read with lucid_get_info) and the affected bins are
+ * painted red, as the reference paints overflowing high-load bins red
+ * (data/shaders/raster_high.glsl:313-317).
+ *
+ * Reference interfaces replaced (paths are relative to the LucidRaster source tree):
+ *   LucidRenderer::exConstruct   src/lucid_renderer.cpp:186-317   -> lucid_create
+ *   LucidRenderer::render        src/lucid_renderer.cpp:319-350   -> lucid_render
+ *   LucidRenderer::uploadInstances src/lucid_renderer.cpp:352-429 -> lucid_build_instances
+ *   LucidRenderer::setupInputData src/lucid_renderer.cpp:431-451  -> (inside lucid_quad_setup)
+ *   LucidRenderer::quadSetup     src/lucid_renderer.cpp:453-482   -> lucid_quad_setup
+ *   LucidRenderer::computeBins   src/lucid_renderer.cpp:484-528   -> lucid_bin_count,
+ *                                                                  lucid_bin_categorize,
+ *                                                                  lucid_bin_dispatch
+ *   LucidRenderer::rasterLow/High src/lucid_renderer.cpp:555-580  -> lucid_raster
+ *   LucidRenderer::verifyInfo/getStats src/lucid_renderer.cpp:629-836 -> lucid_get_info
+ *   FrustumInfo(const Camera&)   src/shading.cpp:46-74            -> lucid_make_config
+ */
+#ifndef LUCID_GB300_H
+#define LUCID_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LUCID_ABI_VERSION 1
+
+/* ---------------------------------------------------------------------------------------- */
+/* Constants shared with the reference (data/shaders/shared/definitions.glsl:73-100)          */
+
+#define LUCID_BIN_LEVELS_COUNT 5
+#define LUCID_REJECTION_TYPE_COUNT 4
+#define LUCID_TIMERS_COUNT 8
+#define LUCID_STATS_COUNT 4
+#define LUCID_INFO_MAX_DISPATCHES 256
+
+#define LUCID_BIN_LEVEL_EMPTY 0
+#define LUCID_BIN_LEVEL_MICRO 1
+#define LUCID_BIN_LEVEL_LOW 2
+#define LUCID_BIN_LEVEL_MEDIUM 3
+#define LUCID_BIN_LEVEL_HIGH 4
+
+/* InstanceData.flags bits (definitions.glsl:85-94, DrawCallOpt in src/lucid_base.h:140-142) */
+#define LUCID_INST_HAS_VERTEX_COLORS 0x001u
+#define LUCID_INST_HAS_VERTEX_TEX_COORDS 0x002u
+#define LUCID_INST_HAS_VERTEX_NORMALS 0x004u
+#define LUCID_INST_IS_OPAQUE 0x008u
+#define LUCID_INST_TEX_OPAQUE 0x010u
+#define LUCID_INST_HAS_UV_RECT 0x020u
+#define LUCID_INST_HAS_ALBEDO_TEXTURE 0x040u
+#define LUCID_INST_HAS_NORMAL_TEXTURE 0x080u
+#define LUCID_INST_HAS_PBR_TEXTURE 0x100u
+#define LUCID_INST_HAS_COLOR 0x200u
+
+/* Rejection reasons (definitions.glsl:97-100) */
+#define LUCID_REJECTION_TYPE_OTHER 0
+#define LUCID_REJECTION_TYPE_BACKFACE 1
+#define LUCID_REJECTION_TYPE_FRUSTUM 2
+#define LUCID_REJECTION_TYPE_BETWEEN_SAMPLES 3
+
+/* Largest instance the setup pass accepts (src/lucid_renderer.h:29 max_instance_quads). */
+#define LUCID_MAX_INSTANCE_QUADS 1024
+
+/* ---------------------------------------------------------------------------------------- */
+/* Status codes                                                                              */
+
+typedef enum lucid_status {
+	LUCID_OK = 0,
+	LUCID_INVALID_ARG = 1,
+	LUCID_CAPACITY_EXCEEDED = 2,
+	LUCID_CUDA_ERROR = 3,
+	LUCID_TIMEOUT = 4,
+	LUCID_NOT_SUPPORTED = 5,
+	LUCID_OUT_OF_MEMORY = 6
+} lucid_status;
+
+/* lucid_info.error_code values (device-side, first error wins) */
+#define LUCID_ERR_NONE 0u
+#define LUCID_ERR_VISIBLE_QUADS 1u    /* more visible quads than options.max_visible_quads   */
+#define LUCID_ERR_BIN_REFS 2u         /* bin quad/tri reference lists overflowed             */
+#define LUCID_ERR_BAND_ENTRIES 3u     /* a 4-row band of a bin has too many triangle rows    */
+#define LUCID_ERR_PIXEL_FRAGMENTS 4u  /* one pixel has more fragments than the sort capacity */
+#define LUCID_ERR_INSTANCE_QUADS 5u   /* an instance has more than 1024 quads                */
+#define LUCID_ERR_BIN_COUNT 6u        /* internal: bin work queue inconsistency              */
+#define LUCID_ERR_VERTEX_INDEX 7u     /* a quad index is >= num_verts (quad rejected)        */
+
+/* ---------------------------------------------------------------------------------------- */
+/* Structures with the reference's memory layout                                             */
+
+/* InstanceData (data/shaders/shared/structures.glsl:9-14): 16 bytes. */
+typedef struct lucid_instance {
+	int32_t index_offset;  /* offset (in u32 indices) of the instance's first quad in quads_ib */
+	int32_t vertex_offset; /* added to every index of the instance                           */
+	int32_t num_quads;     /* <= LUCID_MAX_INSTANCE_QUADS                                     */
+	uint32_t flags;        /* LUCID_INST_* bits (low 16 bits used)                            */
+} lucid_instance;
+
+/* Frustum (structures.glsl:24-28), std140: 12 vec4 = 192 bytes. xyz used, w padding. */
+typedef struct lucid_frustum {
+	float ws_origins[4][4];
+	float ws_dirs[4][4];
+	float ws_origin0[4];
+	float ws_dir0[4];
+	float ws_dirx[4];
+	float ws_diry[4];
+} lucid_frustum;
+
+/* Lighting (structures.glsl:16-21), std140: 64 bytes. */
+typedef struct lucid_lighting {
+	float ambient_color[4];
+	float sun_color[4];
+	float sun_dir[4];
+	float sun_power, ambient_power;
+	float _pad[2];
+} lucid_lighting;
+
+/* LucidConfig (structures.glsl:102-111), std140: 352 bytes.
+ * view_proj_matrix is column-major (GLSL mat4: element [col][row] at index col*4+row). */
+typedef struct lucid_config {
+	lucid_frustum frustum;
+	float view_proj_matrix[16];
+	lucid_lighting lighting;
+	float background_color[4];
+	uint32_t enable_backface_culling;
+	int32_t num_instances;
+	int32_t instance_packet_size;
+	uint32_t _pad;
+} lucid_config;
+
+/* LucidInfo (structures.glsl:70-99): identical layout for the first 1152 u32 words, followed
+ * by 64 u32 words of GB300-specific status. In device memory the per-bin counter array
+ * (10 * bin_count u32, definitions.glsl:117-129) follows this structure. */
+typedef struct lucid_info {
+	int32_t num_input_quads;
+	int32_t num_visible_quads[2];
+	int32_t num_counted_quads[2];
+	int32_t bin_level_counts[LUCID_BIN_LEVELS_COUNT];
+
+	uint32_t a_small_bins, a_high_bins;
+	uint32_t a_setup_work_groups;
+	uint32_t a_dummy_counter;
+
+	uint32_t num_binning_dispatches[3];
+	uint32_t bin_level_dispatches[LUCID_BIN_LEVELS_COUNT][3];
+
+	uint32_t num_rejected_quads[LUCID_REJECTION_TYPE_COUNT];
+
+	uint32_t setup_timers[LUCID_TIMERS_COUNT];
+	uint32_t raster_timers[LUCID_TIMERS_COUNT];
+	uint32_t bin_dispatcher_timers[LUCID_TIMERS_COUNT];
+
+	/* stats[0]: fragments, stats[1]: half-block-tris, stats[2]: invalid pixels */
+	uint32_t stats[LUCID_STATS_COUNT];
+
+	int32_t dispatcher_first_batch[2][LUCID_INFO_MAX_DISPATCHES];
+	int32_t dispatcher_num_batches[2][LUCID_INFO_MAX_DISPATCHES];
+
+	int32_t temp[64];
+
+	/* ---- GB300 extension (not in the reference) ---- */
+	uint32_t error_code;      /* LUCID_ERR_*                                               */
+	uint32_t error_detail[3]; /* e.g. bin id / count / capacity of the first error        */
+	uint32_t raster_work_counter;
+	uint32_t num_bin_quad_refs; /* sum of per-bin quad counts                             */
+	uint32_t num_bin_tri_refs;  /* sum of per-bin tri counts                              */
+	uint32_t max_pixel_fragments;
+	uint64_t num_fragments;   /* 64-bit fragment count (stats[0] wraps above 2^32)        */
+	uint64_t num_hblock_tris; /* 64-bit stats[1]                                          */
+	uint32_t num_band_entries;
+	uint32_t num_views;
+	uint32_t ext_reserved[50];
+} lucid_info;
+
+#define LUCID_INFO_REFERENCE_WORDS 1152
+#define LUCID_INFO_WORDS 1216
+
+/* ---------------------------------------------------------------------------------------- */
+/* Renderer options (LucidRenderOpt in src/lucid_renderer.h:10-13 plus GB300 limits)          */
+
+#define LUCID_OPT_TIMERS 0x01u            /* clock64 section timers into lucid_info.*_timers */
+#define LUCID_OPT_ADDITIVE_BLENDING 0x02u /* out += rgb*a (shading.glsl:276-277)               */
+#define LUCID_OPT_ALPHA_THRESHOLD 0x04u   /* stop a pixel once T < 1/128 (shading.glsl:62)     */
+#define LUCID_OPT_VISUALIZE_ERRORS 0x08u  /* reserved (reference-order mode only)              */
+
+typedef struct lucid_options {
+	uint32_t flags;            /* LUCID_OPT_*                                                  */
+	int32_t bin_size;          /* must be 32 (src/lucid_renderer.cpp:190)                      */
+	int32_t max_input_quads;   /* capacity of the per-input-quad classification buffer        */
+	int32_t max_visible_quads; /* MAX_VISIBLE_QUADS (definitions.glsl:54)                      */
+	int32_t max_instances;     /* src/lucid_renderer.h:28 (64K)                                */
+	int32_t low_high_threshold;/* bins with >= this many tris are HIGH (bin_categorizer.glsl:72)*/
+	int32_t max_bin_refs;      /* capacity of each of the bin quad / bin tri lists             */
+	int32_t band_capacity;     /* triangle rows per 4-row band of a bin (raster scratch)       */
+	int32_t binning_ctas;      /* CTAs of bin_count / bin_dispatch (0 = 2 per SM)              */
+	int32_t raster_ctas_per_sm;/* 0 = as many as fit                                           */
+	int32_t max_views;         /* views of lucid_render_batch                                  */
+	int32_t reserved[5];
+} lucid_options;
+
+/* ---------------------------------------------------------------------------------------- */
+/* Per-frame inputs (RenderContext, src/lucid_base.h:72-84, as used by
+ * src/lucid_renderer.cpp:352-451). All array pointers are DEVICE pointers.                   */
+
+#define LUCID_COLOR_RGBA8 0   /* u32 per vertex, R in the low byte (IColor)                   */
+#define LUCID_COLOR_RGBA16F 1 /* 4 x IEEE half per vertex                                     */
+#define LUCID_COLOR_RGBA32F 2 /* 4 x float per vertex                                         */
+
+typedef struct lucid_frame_inputs {
+	const float* positions;          /* float3 per vertex (world space)                         */
+	const void* colors;              /* per-vertex colours, layout given by color_format        */
+	int32_t color_format;            /* LUCID_COLOR_*                                           */
+	int32_t num_verts;
+	const uint32_t* quads_ib;        /* 4 u32 vertex indices per quad; a triangle is (a,b,c,c)  */
+	int32_t num_quads;               /* total input quads = sum of instances' num_quads         */
+	int32_t num_instances;
+	const lucid_instance* instances; /* device array of num_instances                           */
+	const uint32_t* instance_colors; /* RGBA8 per instance (used with LUCID_INST_HAS_COLOR)     */
+	const float* tri_opacity;        /* optional: per input triangle (quad*2+second), may be 0  */
+	const lucid_config* config;      /* HOST pointer, copied into the renderer's buffer         */
+} lucid_frame_inputs;
+
+/* Draw call of the host-side instance builder (SceneDrawCall, src/lucid_base.h:44-50). */
+typedef struct lucid_draw_call {
+	int32_t quad_offset;
+	int32_t num_quads;
+	uint32_t opts;          /* LUCID_INST_* bits of the draw call                                */
+	uint32_t material_color;/* RGBA8; 0xffffffff means "no instance colour"                      */
+} lucid_draw_call;
+
+/* Simple perspective camera used to fill LucidConfig (stands in for libfwk Camera). The camera
+ * looks down -Z of its own frame; pixel (x, y) maps to NDC (2x/W-1, 2y/H-1). */
+typedef struct lucid_camera {
+	float position[3];
+	float right[3], up[3], forward[3]; /* orthonormal basis; forward is the view direction */
+	float fov_y_radians;
+	float near_plane, far_plane;
+} lucid_camera;
+
+/* View of a batched render (no reference counterpart). */
+typedef struct lucid_view {
+	int32_t width, height;
+	lucid_frame_inputs inputs;
+	float* out_rgba; /* device, width*height*4 floats */
+} lucid_view;
+
+typedef struct lucid_renderer lucid_renderer;
+
+/* ---------------------------------------------------------------------------------------- */
+/* Host-only helpers (no GPU needed)                                                         */
+
+const char* lucid_status_string(lucid_status status);
+/* Text of the last error raised on the calling thread (empty string if none). */
+const char* lucid_last_error_string(void);
+int lucid_abi_version(void);
+lucid_status lucid_default_options(lucid_options* out);
+
+/* Splits draw calls into instances of at most 1024 quads, as LucidRenderer::uploadInstances
+ * does (src/lucid_renderer.cpp:352-429). Writes up to max_instances records and returns the
+ * number written in *out_count (truncated like the reference, which resizes to max_instances).
+ * out_colors receives one RGBA8 instance colour per instance (may be NULL). */
+lucid_status lucid_build_instances(const lucid_draw_call* draw_calls, int32_t num_draw_calls,
+								   lucid_instance* out_instances, uint32_t* out_colors,
+								   int32_t max_instances, int32_t* out_count,
+								   int32_t* out_num_quads);
+
+/* Fills a LucidConfig from a camera, as FrustumInfo (src/shading.cpp:46-74) and
+ * LucidRenderer::setupInputData (src/lucid_renderer.cpp:439-446) do. background_rgba may be
+ * NULL (0,0,0,1). Lighting is set to SceneLighting::makeDefault (src/shading.cpp:26-34). */
+lucid_status lucid_make_config(const lucid_camera* camera, int32_t width, int32_t height,
+							   const float* background_rgba, int32_t backface_culling,
+							   lucid_config* out);
+
+/* ---------------------------------------------------------------------------------------- */
+/* Renderer                                                                                  */
+
+lucid_status lucid_create(const lucid_options* options, int32_t width, int32_t height,
+						  lucid_renderer** out);
+lucid_status lucid_destroy(lucid_renderer* renderer);
+
+/* Whole frame: quad setup, bin count, categorize, dispatch, raster. Asynchronous on `stream`,
+ * no host synchronisation, graph-capturable. out_rgba: device, width*height*4 floats, row y
+ * of the image at offset y*width*4. */
+lucid_status lucid_render(lucid_renderer* renderer, const lucid_frame_inputs* inputs,
+						  float* out_rgba, void* stream);
+
+/* Pass-level entry points (one per reference compute pass). They operate on the renderer's
+ * buffers, so a caller can inspect intermediates between them. lucid_quad_setup also resets
+ * the info block and uploads the config (setupInputData). */
+lucid_status lucid_quad_setup(lucid_renderer* renderer, const lucid_frame_inputs* inputs,
+							  void* stream);
+lucid_status lucid_bin_count(lucid_renderer* renderer, void* stream);
+lucid_status lucid_bin_categorize(lucid_renderer* renderer, void* stream);
+lucid_status lucid_bin_dispatch(lucid_renderer* renderer, void* stream);
+lucid_status lucid_raster(lucid_renderer* renderer, const lucid_frame_inputs* inputs,
+						  float* out_rgba, void* stream);
+
+/* Synchronises `stream` and copies the info block (and, if bin_counters is non-NULL, the
+ * 10*bin_count per-bin counters) to host memory. */
+lucid_status lucid_get_info(lucid_renderer* renderer, lucid_info* out_info,
+							uint32_t* bin_counters, void* stream);
+
+/* Read-only view of internal buffers, for parity tests and statistics. Synchronises `stream`
+ * and copies min(bytes, buffer size) bytes of buffer `which` into host_dst. *out_bytes (may be
+ * NULL) receives the buffer's size. */
+#define LUCID_BUF_QUAD_AABBS 0    /* u32 per visible quad slot (MAX_VISIBLE_QUADS)             */
+#define LUCID_BUF_TRI_BARY 1      /* uvec4 x2 per tri slot                                     */
+#define LUCID_BUF_TRI_SCAN 2      /* uvec4 x2 per tri slot                                     */
+#define LUCID_BUF_TRI_DEPTH 3     /* uvec4 per tri slot                                        */
+#define LUCID_BUF_QUAD_COLORS 4   /* uvec4 per quad slot (RGBA8 vertex colours)                */
+#define LUCID_BUF_TRI_NORMALS 5   /* u32 per tri slot                                          */
+#define LUCID_BUF_QUAD_SOURCE 6   /* u32 per quad slot: input quad index                       */
+#define LUCID_BUF_BIN_QUADS 7     /* u32 per bin quad reference                                */
+#define LUCID_BUF_BIN_TRIS 8      /* u32 per bin tri reference                                 */
+#define LUCID_BUF_QUAD_VERTS 9    /* uvec4 per quad slot: vertex indices                       */
+lucid_status lucid_download_buffer(lucid_renderer* renderer, int32_t which, void* host_dst,
+								   size_t bytes, size_t* out_bytes, void* stream);
+
+/* Verification mode of the raster pass: renders like lucid_raster and also records, for each
+ * pixel, the number of fragments and the input primitive ids (quad*2+second) of its first
+ * max_per_pixel fragments in exact blend order (nearest first, ties by primitive id).
+ * Host outputs: counts[width*height], prims[width*height*max_per_pixel]. Synchronous. */
+lucid_status lucid_raster_dump(lucid_renderer* renderer, const lucid_frame_inputs* inputs,
+							   float* out_rgba, int32_t max_per_pixel, int32_t* host_counts,
+							   int32_t* host_prims, void* stream);
+
+/* Backward pass (no reference counterpart): given dL/dimage (device, width*height*4 floats,
+ * alpha channel ignored), accumulates dL/d(vertex RGBA) into dvertex_rgba (device,
+ * num_verts*4 floats; only for LUCID_COLOR_RGBA32F colours) and dL/d(triangle opacity) into
+ * dtri_opacity (device, num_quads*2 floats; requires inputs->tri_opacity). Either output may
+ * be NULL. Gradients are ADDED to the buffers. Requires a prior lucid_render (or the full pass
+ * sequence) of the same inputs on this renderer; fragment lists are recomputed, not stored. */
+lucid_status lucid_render_backward(lucid_renderer* renderer, const lucid_frame_inputs* inputs,
+								   const float* dl_dimage, float* dvertex_rgba,
+								   float* dtri_opacity, void* stream);
+
+/* Batched forward (no reference counterpart): renders num_views independent views (each with
+ * its own size, geometry and config) with one launch per pass for all views. The renderer must
+ * have been created with options.max_views >= num_views and width/height at least as large as
+ * every view. views is a HOST array. */
+lucid_status lucid_render_batch(lucid_renderer* renderer, const lucid_view* views,
+								int32_t num_views, void* stream);
+
+/* Picks raster launch parameters by timing candidate configurations on `inputs`; stores the
+ * winner in the renderer and returns it in *out_ctas_per_sm / *out_low_high_threshold. */
+lucid_status lucid_autotune(lucid_renderer* renderer, const lucid_frame_inputs* inputs,
+							float* scratch_rgba, int32_t* out_ctas_per_sm,
+							int32_t* out_low_high_threshold, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LUCID_GB300_H */

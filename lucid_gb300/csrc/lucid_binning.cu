@@ -1,0 +1,316 @@
+// Binning passes: data/shaders/bin_counter.glsl, bin_categorizer.glsl, bin_dispatcher.glsl.
+//
+// binCountKernel      fixed grid of CTAs; CTA c owns a contiguous range of the visible small
+//                     quads and of the visible large quads. Shared-memory histogram per bin,
+//                     written to the CTA's row of bin_batches (the reference keeps the same
+//                     per-work-group histograms, bin_counter.glsl:184-190) and added to the
+//                     global BIN_QUAD_COUNTS / BIN_TRI_COUNTS.
+//                     Small quads count every bin of their AABB; large triangles count bin
+//                     rows by the conservative bin scanline (scanline.glsl:28-52) as a +1/-1
+//                     difference array closed by a warp prefix scan per row.
+// binCategorizeKernel one CTA: exclusive scans of the counts (offsets), LOW/HIGH bin lists in
+//                     bin order, level counts and the raster work list (HIGH, LOW, EMPTY).
+// binDispatchKernel   same CTA ranges as the counter; each CTA reserves its slice of every bin
+//                     once (atomicAdd on *_OFFSETS_TEMP) and scatters quad / tri references.
+//
+// The order of references inside one bin depends on shared-memory atomics (as in the
+// reference); every consumer is order-independent and tests compare lists per bin sorted.
+
+#include "lucid_common.cuh"
+#include "lucid_kernels.h"
+
+namespace lucid {
+
+struct BinScan {
+	float mn[3], mx[3], step[3];
+};
+
+// scanline.glsl:28-52 (loadScanlineParamsBin)
+__device__ __forceinline__ BinScan loadScanlineParamsBin(uint4 r0, uint4 r1, int& min_by,
+														 int& max_by) {
+	BinScan s;
+	float scan[3] = {bitsf(r0.x), bitsf(r0.y), bitsf(r0.z)};
+	s.step[0] = bitsf(r1.x), s.step[1] = bitsf(r1.y), s.step[2] = bitsf(r1.z);
+	min_by = int(r0.w & 0xffffu) >> kBinShift;
+	max_by = int(r0.w >> 16) >> kBinShift;
+	const float offset = float(kBinSize) - 0.989f;
+	const float start_x = 0.99f, start_y = float(min_by * kBinSize) - 0.01f;
+#pragma unroll
+	for(int i = 0; i < 3; i++) {
+		bool xneg = (r1.w >> i) & 1u, yneg = (r1.w >> (3 + i)) & 1u;
+		float yoff = yneg ? 0.0f : offset, xoff = xneg ? 0.0f : offset;
+		scan[i] = scan[i] + (s.step[i] * (yoff + start_y) - (xoff + start_x));
+		s.mn[i] = xneg ? -INFINITY : scan[i];
+		s.mx[i] = xneg ? scan[i] : INFINITY;
+		s.step[i] = s.step[i] * float(kBinSize);
+	}
+	return s;
+}
+
+// bin_counter.glsl:53-62 (scanlineStep)
+__device__ __forceinline__ void scanlineStep(BinScan& s, int& bmin, int& bmax) {
+	float xmin = fmaxf(fmaxf(s.mn[0], s.mn[1]), s.mn[2]);
+	float xmax = fminf(fminf(s.mx[0], s.mx[1]), s.mx[2]);
+#pragma unroll
+	for(int i = 0; i < 3; i++)
+		s.mn[i] += s.step[i], s.mx[i] += s.step[i];
+	bmin = f2i(xmin + 1.0f) >> kBinShift;
+	bmax = f2i(xmax) >> kBinShift;
+}
+
+__device__ __forceinline__ void ctaRange(int n, int& beg, int& end) {
+	beg = int((int64_t(n) * blockIdx.x) / gridDim.x);
+	end = int((int64_t(n) * (blockIdx.x + 1)) / gridDim.x);
+}
+
+// ---------------------------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(kBinningThreads, 1) binCountKernel(FrameParams p) {
+	extern __shared__ int s_bins[];
+	const int bins = p.bin_count, bcx = p.bin_count_x, bcy = p.bin_count_y;
+	const int mvq = p.max_visible_quads;
+	const int nsmall = p.info->num_visible_quads[0], nlarge = p.info->num_visible_quads[1];
+	int* hist = p.bin_batches + size_t(blockIdx.x) * 2 * bins;
+
+	// ---- small quads: every bin of the AABB (bin_counter.glsl:64-80)
+	for(int i = threadIdx.x; i < bins; i += blockDim.x)
+		s_bins[i] = 0;
+	__syncthreads();
+	int sbeg, send;
+	ctaRange(nsmall, sbeg, send);
+	for(int k = sbeg + threadIdx.x; k < send; k += blockDim.x) {
+		int x0, y0, x1, y1;
+		decodeAABB28(p.quad_aabbs[k], x0, y0, x1, y1);
+		for(int by = y0; by <= y1; by++)
+			for(int bx = x0; bx <= x1; bx++)
+				atomicAdd(&s_bins[by * bcx + bx], 1);
+	}
+	__syncthreads();
+	for(int i = threadIdx.x; i < bins; i += blockDim.x) {
+		int v = s_bins[i];
+		hist[i] = v;
+		if(v > 0)
+			atomicAdd(&binQuadCounts(p, i), uint32_t(v));
+	}
+	__syncthreads();
+
+	// ---- large tris: bin rows by scanline (bin_counter.glsl:112-134)
+	for(int i = threadIdx.x; i < bins; i += blockDim.x)
+		s_bins[i] = 0;
+	__syncthreads();
+	int lbeg, lend;
+	ctaRange(nlarge, lbeg, lend);
+	int items = 2 * (lend - lbeg);
+	for(int it = threadIdx.x; it < items; it += blockDim.x) {
+		int k = lbeg + (it >> 1), second = it & 1;
+		int quad_idx = (mvq - 1) - k;
+		uint32_t enc = p.quad_aabbs[quad_idx];
+		if((enc >> (30 + second)) & 1u)
+			continue;
+		uint32_t tri = uint32_t(quad_idx) * 2 + second;
+		int x0, y0, x1, y1;
+		decodeAABB28(enc, x0, y0, x1, y1);
+		int bsy, bey;
+		BinScan sc = loadScanlineParamsBin(p.tri_scan[size_t(tri) * 2], p.tri_scan[size_t(tri) * 2 + 1],
+										   bsy, bey);
+		for(int by = bsy; by <= bey; by++) {
+			int bmin, bmax;
+			scanlineStep(sc, bmin, bmax);
+			bmin = max(bmin, x0), bmax = min(bmax, x1);
+			if(bmax >= bmin) {
+				atomicAdd(&s_bins[bmin + by * bcx], 1);
+				if(bmax + 1 < bcx)
+					atomicAdd(&s_bins[bmax + 1 + by * bcx], -1);
+			}
+		}
+	}
+	__syncthreads();
+	// close the difference arrays: one warp per bin row (bin_counter.glsl:82-103)
+	{
+		int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+		for(int by = warp; by < bcy; by += nw) {
+			int prev = 0;
+			for(int base = 0; base < bcx; base += 32) {
+				int bx = base + lane;
+				int v = bx < bcx ? s_bins[by * bcx + bx] : 0;
+				int acc = prev + warpInclusiveScan(v);
+				if(bx < bcx)
+					s_bins[by * bcx + bx] = acc;
+				prev = __shfl_sync(0xffffffffu, acc, 31);
+			}
+		}
+	}
+	__syncthreads();
+	for(int i = threadIdx.x; i < bins; i += blockDim.x) {
+		int v = s_bins[i];
+		hist[bins + i] = v;
+		if(v > 0)
+			atomicAdd(&binTriCounts(p, i), uint32_t(v));
+	}
+	if(threadIdx.x < 2 && blockIdx.x < LUCID_INFO_MAX_DISPATCHES) {
+		int batch = threadIdx.x == 0 ? 4096 : 512;
+		int beg = threadIdx.x == 0 ? sbeg : lbeg, end = threadIdx.x == 0 ? send : lend;
+		p.info->dispatcher_first_batch[threadIdx.x][blockIdx.x] = end > beg ? beg / batch : -1;
+		p.info->dispatcher_num_batches[threadIdx.x][blockIdx.x] = (end - beg + batch - 1) / batch;
+	}
+	if(blockIdx.x == 0 && threadIdx.x == 0) {
+		// quad_setup.glsl:471-485
+		int tasks = (nsmall + 4095) / 4096 + (nlarge + 511) / 512;
+		p.info->num_binning_dispatches[0] = uint32_t(min(max(tasks, 4), kMaxDispatches));
+		p.info->num_binning_dispatches[1] = 1;
+		p.info->num_binning_dispatches[2] = 1;
+		p.info->num_counted_quads[0] = nsmall;
+		p.info->num_counted_quads[1] = nlarge;
+	}
+}
+
+// ---------------------------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(1024) binCategorizeKernel(FrameParams p) {
+	__shared__ uint32_t s_scan[33];
+	__shared__ int s_iscan[33];
+	const int bins = p.bin_count;
+	const int per = (bins + blockDim.x - 1) / blockDim.x;
+	const int beg = min(bins, int(threadIdx.x) * per), end = min(bins, beg + per);
+
+	// bin_categorizer.glsl:22-53: exclusive scans into *_OFFSETS and *_OFFSETS_TEMP
+	uint32_t lq = 0, lt = 0;
+	int nlow = 0, nhigh = 0, nempty = 0;
+	for(int i = beg; i < end; i++) {
+		uint32_t q = binQuadCounts(p, i), t = binTriCounts(p, i);
+		lq += q, lt += t;
+		int64_t num_tris = int64_t(t) + int64_t(q) * 2;
+		if(num_tris == 0)
+			nempty++;
+		else if(num_tris < p.low_high_threshold)
+			nlow++;
+		else
+			nhigh++;
+	}
+	uint32_t tq, tt;
+	uint32_t oq = blockExclusiveScan(lq, s_scan, &tq);
+	uint32_t ot = blockExclusiveScan(lt, s_scan, &tt);
+	int tlow, thigh, tempty;
+	int olow = blockExclusiveScan(nlow, s_iscan, &tlow);
+	int ohigh = blockExclusiveScan(nhigh, s_iscan, &thigh);
+	int oempty = blockExclusiveScan(nempty, s_iscan, &tempty);
+	// bin_categorizer.glsl:57-89: levels (EMPTY, LOW < threshold, HIGH), lists in bin order
+	for(int i = beg; i < end; i++) {
+		uint32_t q = binQuadCounts(p, i), t = binTriCounts(p, i);
+		binQuadOffsets(p, i) = oq;
+		binQuadOffsetsTemp(p, i) = oq;
+		binTriOffsets(p, i) = ot;
+		binTriOffsetsTemp(p, i) = ot;
+		oq += q, ot += t;
+		int64_t num_tris = int64_t(t) + int64_t(q) * 2;
+		if(num_tris == 0) {
+			p.raster_work[thigh + tlow + oempty++] = uint32_t(i);
+		} else if(num_tris < p.low_high_threshold) {
+			lowLevelBins(p, olow) = uint32_t(i);
+			p.raster_work[thigh + olow] = uint32_t(i);
+			olow++;
+		} else {
+			highLevelBins(p, ohigh) = uint32_t(i);
+			p.raster_work[ohigh] = uint32_t(i);
+			ohigh++;
+		}
+	}
+	if(threadIdx.x < LUCID_BIN_LEVELS_COUNT) {
+		int lv = threadIdx.x;
+		int cnt = lv == LUCID_BIN_LEVEL_EMPTY ? tempty
+				  : lv == LUCID_BIN_LEVEL_LOW ? tlow
+				  : lv == LUCID_BIN_LEVEL_HIGH ? thigh
+											  : 0;
+		p.info->bin_level_counts[lv] = cnt;
+		int maxd = kMaxDispatches >> (lv == LUCID_BIN_LEVEL_HIGH ? 1 : 0);
+		p.info->bin_level_dispatches[lv][0] = uint32_t(min(cnt, maxd));
+		p.info->bin_level_dispatches[lv][1] = 1;
+		p.info->bin_level_dispatches[lv][2] = 1;
+	}
+	if(threadIdx.x == 0) {
+		p.info->num_bin_quad_refs = tq;
+		p.info->num_bin_tri_refs = tt;
+		if(tq > uint32_t(p.max_bin_refs) || tt > uint32_t(p.max_bin_refs))
+			raiseError(p.info, LUCID_ERR_BIN_REFS, tq, tt, uint32_t(p.max_bin_refs));
+	}
+}
+
+// ---------------------------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(kBinningThreads, 1) binDispatchKernel(FrameParams p) {
+	extern __shared__ int s_bins[];
+	const int bins = p.bin_count, bcx = p.bin_count_x;
+	const int mvq = p.max_visible_quads;
+	const uint32_t cap = uint32_t(p.max_bin_refs);
+	const int nsmall = p.info->num_visible_quads[0], nlarge = p.info->num_visible_quads[1];
+	const int* hist = p.bin_batches + size_t(blockIdx.x) * 2 * bins;
+
+	// ---- small quads (bin_dispatcher.glsl:66-80, 202-232)
+	for(int i = threadIdx.x; i < bins; i += blockDim.x) {
+		int v = hist[i];
+		s_bins[i] = v > 0 ? int(atomicAdd(&binQuadOffsetsTemp(p, i), uint32_t(v))) : 0;
+	}
+	__syncthreads();
+	int sbeg, send;
+	ctaRange(nsmall, sbeg, send);
+	for(int k = sbeg + threadIdx.x; k < send; k += blockDim.x) {
+		uint32_t enc = p.quad_aabbs[k];
+		uint32_t entry = uint32_t(k) | (enc & 0xf0000000u);
+		int x0, y0, x1, y1;
+		decodeAABB28(enc, x0, y0, x1, y1);
+		for(int by = y0; by <= y1; by++)
+			for(int bx = x0; bx <= x1; bx++) {
+				uint32_t slot = uint32_t(atomicAdd(&s_bins[by * bcx + bx], 1));
+				if(slot < cap)
+					p.bin_quads[slot] = entry;
+			}
+	}
+	__syncthreads();
+
+	// ---- large tris (bin_dispatcher.glsl:89-114, 234-258)
+	for(int i = threadIdx.x; i < bins; i += blockDim.x) {
+		int v = hist[bins + i];
+		s_bins[i] = v > 0 ? int(atomicAdd(&binTriOffsetsTemp(p, i), uint32_t(v))) : 0;
+	}
+	__syncthreads();
+	int lbeg, lend;
+	ctaRange(nlarge, lbeg, lend);
+	int items = 2 * (lend - lbeg);
+	for(int it = threadIdx.x; it < items; it += blockDim.x) {
+		int k = lbeg + (it >> 1), second = it & 1;
+		int quad_idx = (mvq - 1) - k;
+		uint32_t enc = p.quad_aabbs[quad_idx];
+		if((enc >> (30 + second)) & 1u)
+			continue;
+		uint32_t tri = uint32_t(quad_idx) * 2 + second;
+		int x0, y0, x1, y1;
+		decodeAABB28(enc, x0, y0, x1, y1);
+		int bsy, bey;
+		BinScan sc = loadScanlineParamsBin(p.tri_scan[size_t(tri) * 2], p.tri_scan[size_t(tri) * 2 + 1],
+										   bsy, bey);
+		for(int by = bsy; by <= bey; by++) {
+			int bmin, bmax;
+			scanlineStep(sc, bmin, bmax);
+			bmin = max(bmin, x0), bmax = min(bmax, x1);
+			for(int bx = bmin; bx <= bmax; bx++) {
+				uint32_t slot = uint32_t(atomicAdd(&s_bins[by * bcx + bx], 1));
+				if(slot < cap)
+					p.bin_tris[slot] = tri;
+			}
+		}
+	}
+}
+
+// ---------------------------------------------------------------------------------------------
+
+void launchBinCount(const FrameParams& p, cudaStream_t stream) {
+	binCountKernel<<<p.num_binning_ctas, kBinningThreads, p.bin_count * sizeof(int), stream>>>(p);
+}
+void launchBinCategorize(const FrameParams& p, cudaStream_t stream) {
+	binCategorizeKernel<<<1, 1024, 0, stream>>>(p);
+}
+void launchBinDispatch(const FrameParams& p, cudaStream_t stream) {
+	binDispatchKernel<<<p.num_binning_ctas, kBinningThreads, p.bin_count * sizeof(int), stream>>>(p);
+}
+
+} // namespace lucid

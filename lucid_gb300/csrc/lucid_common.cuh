@@ -1,0 +1,199 @@
+// Shared device-side definitions of the lucid_gb300 CUDA path.
+//
+// Numerics: every file is compiled with --fmad=false, IEEE division and square root and no
+// flush-to-zero, so each float expression below rounds exactly like the same expression on
+// the CPU. Expressions keep the evaluation order of the reference GLSL (left to right).
+#pragma once
+
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/lucid_gb300.h"
+
+namespace lucid {
+
+constexpr int kBinSize = 32;
+constexpr int kBinShift = 5;
+constexpr int kMaxDispatches = 256;      // LucidRenderer::m_max_dispatches for >= 4 GB
+constexpr int kMaxBinCount = 16384;      // bins of one view (128 x 128 bins = 4096^2 pixels)
+constexpr int kSetupThreads = 256;
+constexpr int kBinningThreads = 1024;
+constexpr int kRasterThreads = 512;
+
+// Per-view device parameters (passed by value to every kernel).
+struct FrameParams {
+	// ---- caller-owned inputs ----
+	const float* positions;
+	const void* colors;
+	int color_format;
+	int num_verts;
+	const uint32_t* quads_ib;
+	int num_quads;
+	int num_instances;
+	const lucid_instance* instances;
+	const uint32_t* instance_colors;
+	const float* tri_opacity;
+	float* out_rgba;
+	// ---- dimensions & limits ----
+	int width, height;
+	int bin_count_x, bin_count_y, bin_count;
+	int max_visible_quads;
+	int max_bin_refs;
+	int band_capacity;
+	int low_high_threshold;
+	int num_setup_ctas;
+	int num_binning_ctas;
+	uint32_t flags;
+	// LucidConfig by value: kernels read it from the parameter bank (no upload needed, so a
+	// frame is graph-capturable without host staging buffers).
+	lucid_config cfg;
+	// ---- renderer-owned buffers ----
+	lucid_info* info;
+	uint32_t* counts;           // 10 * bin_count words after the info block
+	int* inst_offsets;          // num_instances + 1
+	uint4* quad_class;          // per input quad
+	int4* setup_cta_counts;     // per setup CTA: small, large, (unused), (unused)
+	int4* setup_cta_offsets;
+	uint32_t* quad_aabbs;
+	uint32_t* quad_source;
+	uint4* quad_verts;
+	uint4* quad_colors;
+	uint4* tri_bary;  // 2 per tri
+	uint4* tri_scan;  // 2 per tri
+	uint4* tri_depth; // 1 per tri
+	uint32_t* tri_normals;
+	uint32_t* bin_quads;
+	uint32_t* bin_tris;
+	int* bin_batches;     // num_binning_ctas * 2 * bin_count histograms
+	uint32_t* raster_work; // bin_count bin ids: HIGH, LOW, EMPTY
+	uint2* band_scratch;  // per raster CTA: 8 * band_capacity entries
+	int* dump_counts;     // verification mode (may be null)
+	int* dump_prims;
+	int dump_max;
+};
+
+// Offsets into the per-bin counter array (definitions.glsl:117-129)
+__device__ __forceinline__ uint32_t& binQuadCounts(const FrameParams& p, int i) { return p.counts[p.bin_count * 0 + i]; }
+__device__ __forceinline__ uint32_t& binQuadOffsets(const FrameParams& p, int i) { return p.counts[p.bin_count * 1 + i]; }
+__device__ __forceinline__ uint32_t& binQuadOffsetsTemp(const FrameParams& p, int i) { return p.counts[p.bin_count * 2 + i]; }
+__device__ __forceinline__ uint32_t& binTriCounts(const FrameParams& p, int i) { return p.counts[p.bin_count * 3 + i]; }
+__device__ __forceinline__ uint32_t& binTriOffsets(const FrameParams& p, int i) { return p.counts[p.bin_count * 4 + i]; }
+__device__ __forceinline__ uint32_t& binTriOffsetsTemp(const FrameParams& p, int i) { return p.counts[p.bin_count * 5 + i]; }
+__device__ __forceinline__ uint32_t& lowLevelBins(const FrameParams& p, int i) { return p.counts[p.bin_count * 7 + i]; }
+__device__ __forceinline__ uint32_t& highLevelBins(const FrameParams& p, int i) { return p.counts[p.bin_count * 9 + i]; }
+
+// ---------------------------------------------------------------------------------------------
+// Arithmetic helpers (identical evaluation order to the CPU oracle)
+
+struct F3 {
+	float x, y, z;
+};
+__device__ __forceinline__ F3 f3(float x, float y, float z) { return F3{x, y, z}; }
+__device__ __forceinline__ F3 operator-(F3 a, F3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ F3 operator+(F3 a, F3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ F3 operator*(F3 a, float s) { return f3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ bool feq(F3 a, F3 b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
+__device__ __forceinline__ float dot3(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ F3 cross3(F3 a, F3 b) {
+	return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ F3 xyz4(const float* v) { return f3(v[0], v[1], v[2]); }
+
+// GLSL int()/uint() of a float: truncation, saturating, NaN -> 0.
+__device__ __forceinline__ int f2i(float x) {
+	if(x != x)
+		return 0;
+	return __float2int_rz(x);
+}
+__device__ __forceinline__ uint32_t f2u(float x) {
+	if(x != x || x <= 0.0f)
+		return 0u;
+	return __float2uint_rz(x);
+}
+__device__ __forceinline__ uint32_t fbits(float f) { return __float_as_uint(f); }
+__device__ __forceinline__ float bitsf(uint32_t u) { return __uint_as_float(u); }
+
+// Ascending sort key that puts the nearest fragment (largest inv_ray_pos) first.
+__device__ __forceinline__ uint32_t nearFirstKey(float inv_ray_pos) {
+	uint32_t u = fbits(inv_ray_pos);
+	uint32_t asc = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+	return ~asc;
+}
+__device__ __forceinline__ float keyToDepth(uint32_t key) {
+	uint32_t asc = ~key;
+	uint32_t u = (asc & 0x80000000u) ? (asc & 0x7fffffffu) : ~asc;
+	return bitsf(u);
+}
+
+// funcs.glsl:52-59
+__device__ __forceinline__ uint32_t encodeAABB28(uint32_t x0, uint32_t y0, uint32_t x1, uint32_t y1) {
+	return (x0 & 0x7fu) | ((y0 & 0x7fu) << 7) | ((x1 & 0x7fu) << 14) | ((y1 & 0x7fu) << 21);
+}
+__device__ __forceinline__ void decodeAABB28(uint32_t a, int& x0, int& y0, int& x1, int& y1) {
+	x0 = int(a & 0x7fu), y0 = int((a >> 7) & 0x7fu), x1 = int((a >> 14) & 0x7fu),
+	y1 = int((a >> 21) & 0x7fu);
+}
+// funcs.glsl:100-104
+__device__ __forceinline__ float4 decodeRGBA8(uint32_t c) {
+	const float s = 1.0f / 255.0f;
+	return make_float4(float(c & 0xffu) * s, float((c >> 8) & 0xffu) * s,
+					   float((c >> 16) & 0xffu) * s, float((c >> 24) & 0xffu) * s);
+}
+
+// First error wins; details recorded once.
+__device__ __forceinline__ void raiseError(lucid_info* info, uint32_t code, uint32_t d0,
+										   uint32_t d1, uint32_t d2) {
+	if(atomicCAS(&info->error_code, 0u, code) == 0u) {
+		info->error_detail[0] = d0;
+		info->error_detail[1] = d1;
+		info->error_detail[2] = d2;
+	}
+}
+
+// ---------------------------------------------------------------------------------------------
+// Block-wide scans
+
+__device__ __forceinline__ uint32_t laneMaskLt() {
+	uint32_t m;
+	asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+	return m;
+}
+
+template <typename T> __device__ __forceinline__ T warpInclusiveScan(T v) {
+	int lane = threadIdx.x & 31;
+#pragma unroll
+	for(int o = 1; o < 32; o <<= 1) {
+		T t = __shfl_up_sync(0xffffffffu, v, o);
+		if(lane >= o)
+			v += t;
+	}
+	return v;
+}
+
+// Exclusive scan over the block; `smem` needs blockDim.x/32 + 1 elements. Returns the block
+// total in *total. Must be called by all threads of the block.
+template <typename T>
+__device__ __forceinline__ T blockExclusiveScan(T v, T* smem, T* total) {
+	int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+	T inc = warpInclusiveScan(v);
+	if(lane == 31)
+		smem[warp] = inc;
+	__syncthreads();
+	if(warp == 0) {
+		T w = lane < nw ? smem[lane] : T(0);
+		T wi = warpInclusiveScan(w);
+		if(lane < nw)
+			smem[lane] = wi - w;
+		if(lane == nw - 1)
+			smem[nw] = wi;
+	}
+	__syncthreads();
+	T res = smem[warp] + inc - v;
+	if(total)
+		*total = smem[nw];
+	__syncthreads();
+	return res;
+}
+
+} // namespace lucid

@@ -1,0 +1,629 @@
+// C ABI of lucid_gb300: renderer object, buffer arena and pass orchestration.
+//
+// Mirrors LucidRenderer (src/lucid_renderer.h:21-96, src/lucid_renderer.cpp:186-580): the
+// renderer owns every intermediate buffer; a frame is setup -> bin count -> categorize ->
+// dispatch -> raster, all asynchronous on the caller's stream. Unlike the reference, grid
+// sizes never depend on device-side counts (fixed or persistent grids read the counts on the
+// device), so a frame needs no indirect dispatch and can be captured in a CUDA graph.
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "lucid_common.cuh"
+#include "lucid_kernels.h"
+
+namespace lucid {
+cudaError_t configureRasterKernel();
+}
+
+using namespace lucid;
+
+static_assert(sizeof(lucid_instance) == 16, "InstanceData layout");
+static_assert(sizeof(lucid_frustum) == 192, "Frustum layout");
+static_assert(sizeof(lucid_lighting) == 64, "Lighting layout");
+static_assert(sizeof(lucid_config) == 352, "LucidConfig layout");
+static_assert(offsetof(lucid_config, view_proj_matrix) == 192, "LucidConfig layout");
+static_assert(offsetof(lucid_config, lighting) == 256, "LucidConfig layout");
+static_assert(offsetof(lucid_config, background_color) == 320, "LucidConfig layout");
+static_assert(offsetof(lucid_config, enable_backface_culling) == 336, "LucidConfig layout");
+static_assert(offsetof(lucid_info, temp) == (LUCID_INFO_REFERENCE_WORDS - 64) * 4, "LucidInfo layout");
+static_assert(offsetof(lucid_info, error_code) == LUCID_INFO_REFERENCE_WORDS * 4, "LucidInfo layout");
+static_assert(sizeof(lucid_info) == LUCID_INFO_WORDS * 4, "lucid_info size");
+static_assert(offsetof(lucid_info, num_fragments) % 8 == 0, "64-bit counters alignment");
+
+namespace {
+
+thread_local std::string g_last_error;
+
+lucid_status fail(lucid_status st, const std::string& msg) {
+	g_last_error = msg;
+	return st;
+}
+
+lucid_status cudaFail(cudaError_t err, const char* what) {
+	return fail(LUCID_CUDA_ERROR, std::string(what) + ": " + cudaGetErrorString(err));
+}
+
+#define LUCID_CUDA_TRY(call)                                                                       \
+	do {                                                                                           \
+		cudaError_t err__ = (call);                                                                \
+		if(err__ != cudaSuccess)                                                                   \
+			return cudaFail(err__, #call);                                                         \
+	} while(0)
+
+template <typename T> size_t bytesOf(size_t n) { return n * sizeof(T); }
+
+} // namespace
+
+struct lucid_renderer {
+	lucid_options opts;
+	int width, height;
+	int bin_count_x, bin_count_y, bin_count;
+	int device, num_sms;
+	int raster_ctas;
+	int setup_ctas_max;
+	std::vector<void*> allocations;
+
+	// buffers
+	unsigned char* info_block = nullptr; // lucid_info + 10 * bin_count u32
+	int* inst_offsets = nullptr;
+	uint4* quad_class = nullptr;
+	int4* setup_cta_counts = nullptr;
+	int4* setup_cta_offsets = nullptr;
+	uint32_t* quad_aabbs = nullptr;
+	uint32_t* quad_source = nullptr;
+	uint4* quad_verts = nullptr;
+	uint4* quad_colors = nullptr;
+	uint4* tri_bary = nullptr;
+	uint4* tri_scan = nullptr;
+	uint4* tri_depth = nullptr;
+	uint32_t* tri_normals = nullptr;
+	uint32_t* bin_quads = nullptr;
+	uint32_t* bin_tris = nullptr;
+	int* bin_batches = nullptr;
+	uint32_t* raster_work = nullptr;
+	uint2* band_scratch = nullptr;
+
+	FrameParams last{}; // parameters of the last quad setup (used by the later passes)
+	bool have_frame = false;
+
+	size_t infoBytes() const { return sizeof(lucid_info) + size_t(10) * bin_count * 4; }
+	lucid_info* info() const { return reinterpret_cast<lucid_info*>(info_block); }
+	uint32_t* counts() const { return reinterpret_cast<uint32_t*>(info_block + sizeof(lucid_info)); }
+};
+
+namespace {
+
+template <typename T> lucid_status allocate(lucid_renderer* r, T** ptr, size_t count) {
+	void* p = nullptr;
+	size_t bytes = std::max<size_t>(count * sizeof(T), 16);
+	cudaError_t err = cudaMalloc(&p, bytes);
+	if(err != cudaSuccess) {
+		cudaGetLastError();
+		return fail(LUCID_OUT_OF_MEMORY, std::string("cudaMalloc(") + std::to_string(bytes) +
+											 " bytes): " + cudaGetErrorString(err));
+	}
+	r->allocations.push_back(p);
+	*ptr = reinterpret_cast<T*>(p);
+	return LUCID_OK;
+}
+
+void freeAll(lucid_renderer* r) {
+	for(void* p : r->allocations)
+		cudaFree(p);
+	r->allocations.clear();
+}
+
+lucid_status validateInputs(const lucid_renderer* r, const lucid_frame_inputs* in) {
+	if(!in)
+		return fail(LUCID_INVALID_ARG, "inputs is NULL");
+	if(!in->config)
+		return fail(LUCID_INVALID_ARG, "inputs->config is NULL");
+	if(in->num_quads < 0 || in->num_instances < 0 || in->num_verts < 0)
+		return fail(LUCID_INVALID_ARG, "negative counts in inputs");
+	if(in->num_quads > r->opts.max_input_quads)
+		return fail(LUCID_CAPACITY_EXCEEDED,
+					"num_quads " + std::to_string(in->num_quads) + " > options.max_input_quads " +
+						std::to_string(r->opts.max_input_quads));
+	if(in->num_instances > r->opts.max_instances)
+		return fail(LUCID_CAPACITY_EXCEEDED, "num_instances > options.max_instances");
+	if(in->num_quads > 0 && (!in->positions || !in->quads_ib || !in->instances))
+		return fail(LUCID_INVALID_ARG, "positions, quads_ib and instances are required");
+	if(in->num_quads > 0 && in->num_instances == 0)
+		return fail(LUCID_INVALID_ARG, "num_quads > 0 but no instances");
+	if(in->color_format < LUCID_COLOR_RGBA8 || in->color_format > LUCID_COLOR_RGBA32F)
+		return fail(LUCID_INVALID_ARG, "unknown color_format");
+	if(in->num_quads > 0 && !in->colors)
+		return fail(LUCID_INVALID_ARG, "colors is NULL");
+	return LUCID_OK;
+}
+
+FrameParams makeParams(lucid_renderer* r, const lucid_frame_inputs* in, float* out) {
+	FrameParams p{};
+	p.positions = in->positions;
+	p.colors = in->colors;
+	p.color_format = in->color_format;
+	p.num_verts = in->num_verts;
+	p.quads_ib = in->quads_ib;
+	p.num_quads = in->num_quads;
+	p.num_instances = in->num_instances;
+	p.instances = in->instances;
+	p.instance_colors = in->instance_colors;
+	p.tri_opacity = in->tri_opacity;
+	p.out_rgba = out;
+	p.cfg = *in->config;
+	p.width = r->width, p.height = r->height;
+	p.bin_count_x = r->bin_count_x, p.bin_count_y = r->bin_count_y, p.bin_count = r->bin_count;
+	p.max_visible_quads = r->opts.max_visible_quads;
+	p.max_bin_refs = r->opts.max_bin_refs;
+	p.band_capacity = r->opts.band_capacity;
+	p.low_high_threshold = r->opts.low_high_threshold;
+	p.num_setup_ctas = (in->num_quads + kSetupThreads - 1) / kSetupThreads;
+	p.num_binning_ctas = r->opts.binning_ctas;
+	p.flags = r->opts.flags;
+	p.info = r->info();
+	p.counts = r->counts();
+	p.inst_offsets = r->inst_offsets;
+	p.quad_class = r->quad_class;
+	p.setup_cta_counts = r->setup_cta_counts;
+	p.setup_cta_offsets = r->setup_cta_offsets;
+	p.quad_aabbs = r->quad_aabbs;
+	p.quad_source = r->quad_source;
+	p.quad_verts = r->quad_verts;
+	p.quad_colors = r->quad_colors;
+	p.tri_bary = r->tri_bary;
+	p.tri_scan = r->tri_scan;
+	p.tri_depth = r->tri_depth;
+	p.tri_normals = r->tri_normals;
+	p.bin_quads = r->bin_quads;
+	p.bin_tris = r->bin_tris;
+	p.bin_batches = r->bin_batches;
+	p.raster_work = r->raster_work;
+	p.band_scratch = r->band_scratch;
+	return p;
+}
+
+lucid_status checkLaunch(const char* what) {
+	cudaError_t err = cudaGetLastError();
+	if(err != cudaSuccess)
+		return cudaFail(err, what);
+	return LUCID_OK;
+}
+
+lucid_status resetRasterCounters(lucid_renderer* r, cudaStream_t st) {
+	lucid_info* info = r->info();
+	LUCID_CUDA_TRY(cudaMemsetAsync(&info->raster_work_counter, 0, 4, st));
+	LUCID_CUDA_TRY(cudaMemsetAsync(&info->stats[0], 0, 8, st));
+	LUCID_CUDA_TRY(cudaMemsetAsync(&info->max_pixel_fragments, 0, 4, st));
+	LUCID_CUDA_TRY(cudaMemsetAsync(&info->num_fragments, 0, 16, st));
+	return LUCID_OK;
+}
+
+} // namespace
+
+// ---------------------------------------------------------------------------------------------
+// Host-only helpers
+
+extern "C" const char* lucid_status_string(lucid_status status) {
+	switch(status) {
+	case LUCID_OK: return "ok";
+	case LUCID_INVALID_ARG: return "invalid argument";
+	case LUCID_CAPACITY_EXCEEDED: return "capacity exceeded";
+	case LUCID_CUDA_ERROR: return "CUDA error";
+	case LUCID_TIMEOUT: return "timeout";
+	case LUCID_NOT_SUPPORTED: return "not supported";
+	case LUCID_OUT_OF_MEMORY: return "out of memory";
+	}
+	return "unknown status";
+}
+
+extern "C" const char* lucid_last_error_string(void) { return g_last_error.c_str(); }
+extern "C" int lucid_abi_version(void) { return LUCID_ABI_VERSION; }
+
+extern "C" lucid_status lucid_default_options(lucid_options* out) {
+	if(!out)
+		return fail(LUCID_INVALID_ARG, "out is NULL");
+	memset(out, 0, sizeof(*out));
+	out->flags = 0;
+	out->bin_size = 32;
+	out->max_input_quads = 1 << 22;
+	out->max_visible_quads = 1 << 22;
+	out->max_instances = 64 * 1024;
+	out->low_high_threshold = 1024;
+	out->max_bin_refs = 1 << 24;
+	out->band_capacity = 16384;
+	out->binning_ctas = 0;
+	out->raster_ctas_per_sm = 0;
+	out->max_views = 1;
+	return LUCID_OK;
+}
+
+extern "C" lucid_status lucid_build_instances(const lucid_draw_call* dcs, int32_t num_dcs,
+											  lucid_instance* out, uint32_t* out_colors,
+											  int32_t max_instances, int32_t* out_count,
+											  int32_t* out_num_quads) {
+	if((num_dcs > 0 && !dcs) || !out || !out_count || max_instances < 0)
+		return fail(LUCID_INVALID_ARG, "lucid_build_instances: bad arguments");
+	int n = 0;
+	int64_t total = 0;
+	for(int d = 0; d < num_dcs; d++) {
+		const lucid_draw_call& dc = dcs[d];
+		if(dc.num_quads <= 0)
+			continue;
+		uint32_t opts = dc.opts;
+		if(dc.material_color != 0xffffffffu)
+			opts |= LUCID_INST_HAS_COLOR;
+		for(int i = 0; i < dc.num_quads; i += LUCID_MAX_INSTANCE_QUADS) {
+			if(n < max_instances) {
+				out[n].index_offset = (dc.quad_offset + i) * 4;
+				out[n].vertex_offset = 0;
+				out[n].num_quads = std::min(LUCID_MAX_INSTANCE_QUADS, dc.num_quads - i);
+				out[n].flags = opts & 0xffffu;
+				if(out_colors)
+					out_colors[n] = dc.material_color;
+				total += out[n].num_quads;
+			}
+			n++;
+		}
+	}
+	*out_count = std::min(n, max_instances);
+	if(out_num_quads)
+		*out_num_quads = int32_t(total);
+	if(n > max_instances)
+		return fail(LUCID_CAPACITY_EXCEEDED, "instance limit reached; list truncated");
+	return LUCID_OK;
+}
+
+extern "C" lucid_status lucid_make_config(const lucid_camera* cam, int32_t width, int32_t height,
+										  const float* background, int32_t backface_culling,
+										  lucid_config* out) {
+	if(!cam || !out || width <= 0 || height <= 0)
+		return fail(LUCID_INVALID_ARG, "lucid_make_config: bad arguments");
+	double p[3], r[3], u[3], f[3];
+	for(int i = 0; i < 3; i++)
+		p[i] = cam->position[i], r[i] = cam->right[i], u[i] = cam->up[i], f[i] = cam->forward[i];
+	double ty = tan(double(cam->fov_y_radians) * 0.5);
+	double tx = ty * (double(width) / double(height));
+	double dirs[4][3];
+	const double corners[4][2] = {{-1.0, -1.0}, {-1.0, 1.0}, {1.0, 1.0}, {1.0, -1.0}};
+	for(int c = 0; c < 4; c++)
+		for(int i = 0; i < 3; i++)
+			dirs[c][i] = f[i] + r[i] * (corners[c][0] * tx) + u[i] * (corners[c][1] * ty);
+	memset(out, 0, sizeof(*out));
+	for(int c = 0; c < 4; c++)
+		for(int i = 0; i < 3; i++) {
+			out->frustum.ws_dirs[c][i] = float(dirs[c][i]);
+			out->frustum.ws_origins[c][i] = float(p[i]);
+		}
+	for(int i = 0; i < 3; i++) {
+		out->frustum.ws_origin0[i] = float(p[i]);
+		out->frustum.ws_dir0[i] = float(dirs[0][i]);
+		out->frustum.ws_dirx[i] = float((dirs[3][i] - dirs[0][i]) * (1.0 / double(width)));
+		out->frustum.ws_diry[i] = float((dirs[1][i] - dirs[0][i]) * (1.0 / double(height)));
+	}
+	out->frustum.ws_origin0[3] = 1.0f;
+	double zb[3] = {-f[0], -f[1], -f[2]};
+	double view[4][4] = {{r[0], r[1], r[2], -(r[0] * p[0] + r[1] * p[1] + r[2] * p[2])},
+						 {u[0], u[1], u[2], -(u[0] * p[0] + u[1] * p[1] + u[2] * p[2])},
+						 {zb[0], zb[1], zb[2], -(zb[0] * p[0] + zb[1] * p[1] + zb[2] * p[2])},
+						 {0.0, 0.0, 0.0, 1.0}};
+	double n = cam->near_plane, fa = cam->far_plane;
+	double proj[4][4] = {{1.0 / tx, 0.0, 0.0, 0.0},
+						 {0.0, 1.0 / ty, 0.0, 0.0},
+						 {0.0, 0.0, (fa + n) / (n - fa), (2.0 * fa * n) / (n - fa)},
+						 {0.0, 0.0, -1.0, 0.0}};
+	for(int row = 0; row < 4; row++)
+		for(int col = 0; col < 4; col++) {
+			double acc = 0.0;
+			for(int k = 0; k < 4; k++)
+				acc += proj[row][k] * view[k][col];
+			out->view_proj_matrix[col * 4 + row] = float(acc);
+		}
+	// SceneLighting::makeDefault (src/shading.cpp:26-34)
+	const float amb[4] = {0.8f, 0.8f, 0.6f, 1.0f}, sun[4] = {0.8f, 0.8f, 0.8f, 1.0f};
+	const float sdir[4] = {0.842121f, -0.300567f, -0.447763f, 0.0f};
+	for(int i = 0; i < 4; i++) {
+		out->lighting.ambient_color[i] = amb[i];
+		out->lighting.sun_color[i] = sun[i];
+		out->lighting.sun_dir[i] = sdir[i];
+		out->background_color[i] = background ? background[i] : (i == 3 ? 1.0f : 0.0f);
+	}
+	out->lighting.sun_power = 2.5f;
+	out->lighting.ambient_power = 0.4f;
+	out->enable_backface_culling = backface_culling ? 1u : 0u;
+	out->num_instances = 0;
+	out->instance_packet_size = 1;
+	return LUCID_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Renderer lifetime
+
+extern "C" lucid_status lucid_create(const lucid_options* options, int32_t width, int32_t height,
+									 lucid_renderer** out) {
+	if(!out)
+		return fail(LUCID_INVALID_ARG, "out is NULL");
+	*out = nullptr;
+	lucid_options o;
+	if(options)
+		o = *options;
+	else
+		lucid_default_options(&o);
+	if(o.bin_size != 32)
+		return fail(LUCID_NOT_SUPPORTED, "only 32x32 bins are supported");
+	if(width <= 0 || height <= 0 || width > 4096 || height > 4096)
+		return fail(LUCID_INVALID_ARG, "viewport must be within 1..4096 pixels per axis");
+	if(o.max_visible_quads <= 0 || o.max_visible_quads > (1 << 23) || o.max_input_quads <= 0 ||
+	   o.max_instances <= 0 || o.max_instances > 65536 || o.max_bin_refs <= 0 ||
+	   o.band_capacity <= 0 || o.band_capacity > (1 << 21) || o.low_high_threshold <= 0)
+		return fail(LUCID_INVALID_ARG, "options out of range");
+	if(o.max_views < 1)
+		o.max_views = 1;
+
+	lucid_renderer* r = new lucid_renderer();
+	r->opts = o;
+	r->width = width, r->height = height;
+	r->bin_count_x = (width + kBinSize - 1) / kBinSize;
+	r->bin_count_y = (height + kBinSize - 1) / kBinSize;
+	r->bin_count = r->bin_count_x * r->bin_count_y;
+	auto bail = [&](lucid_status st) {
+		freeAll(r);
+		delete r;
+		return st;
+	};
+	cudaError_t err = cudaGetDevice(&r->device);
+	if(err != cudaSuccess)
+		return bail(cudaFail(err, "cudaGetDevice"));
+	err = cudaDeviceGetAttribute(&r->num_sms, cudaDevAttrMultiProcessorCount, r->device);
+	if(err != cudaSuccess)
+		return bail(cudaFail(err, "cudaDeviceGetAttribute"));
+	if(r->opts.binning_ctas <= 0)
+		r->opts.binning_ctas = 2 * r->num_sms;
+	r->opts.binning_ctas = std::min(r->opts.binning_ctas, 4096);
+	err = configureRasterKernel();
+	if(err != cudaSuccess)
+		return bail(cudaFail(err, "configure raster kernel"));
+	int ctas_per_sm = r->opts.raster_ctas_per_sm > 0 ? r->opts.raster_ctas_per_sm : 1;
+	r->raster_ctas = r->num_sms * ctas_per_sm;
+
+	const size_t mvq = size_t(o.max_visible_quads);
+	const size_t miq = size_t(o.max_input_quads);
+	r->setup_ctas_max = int((miq + kSetupThreads - 1) / kSetupThreads);
+	lucid_status st;
+	if((st = allocate(r, &r->info_block, r->infoBytes())) != LUCID_OK ||
+	   (st = allocate(r, &r->inst_offsets, size_t(o.max_instances) + 1)) != LUCID_OK ||
+	   (st = allocate(r, &r->quad_class, miq)) != LUCID_OK ||
+	   (st = allocate(r, &r->setup_cta_counts, size_t(r->setup_ctas_max))) != LUCID_OK ||
+	   (st = allocate(r, &r->setup_cta_offsets, size_t(r->setup_ctas_max))) != LUCID_OK ||
+	   (st = allocate(r, &r->quad_aabbs, mvq)) != LUCID_OK ||
+	   (st = allocate(r, &r->quad_source, mvq)) != LUCID_OK ||
+	   (st = allocate(r, &r->quad_verts, mvq)) != LUCID_OK ||
+	   (st = allocate(r, &r->quad_colors, mvq)) != LUCID_OK ||
+	   (st = allocate(r, &r->tri_bary, 4 * mvq)) != LUCID_OK ||
+	   (st = allocate(r, &r->tri_scan, 4 * mvq)) != LUCID_OK ||
+	   (st = allocate(r, &r->tri_depth, 2 * mvq)) != LUCID_OK ||
+	   (st = allocate(r, &r->tri_normals, 2 * mvq)) != LUCID_OK ||
+	   (st = allocate(r, &r->bin_quads, size_t(o.max_bin_refs))) != LUCID_OK ||
+	   (st = allocate(r, &r->bin_tris, size_t(o.max_bin_refs))) != LUCID_OK ||
+	   (st = allocate(r, &r->bin_batches, size_t(r->opts.binning_ctas) * 2 * r->bin_count)) != LUCID_OK ||
+	   (st = allocate(r, &r->raster_work, size_t(r->bin_count))) != LUCID_OK ||
+	   (st = allocate(r, &r->band_scratch, size_t(r->raster_ctas) * 8 * o.band_capacity)) != LUCID_OK)
+		return bail(st);
+	// zero the records once so that unused slots read as zero in parity dumps
+	for(void* p : {(void*)r->quad_aabbs, (void*)r->quad_source})
+		cudaMemset(p, 0, mvq * 4);
+	cudaMemset(r->quad_verts, 0, mvq * 16);
+	cudaMemset(r->quad_colors, 0, mvq * 16);
+	cudaMemset(r->tri_bary, 0, mvq * 64);
+	cudaMemset(r->tri_scan, 0, mvq * 64);
+	cudaMemset(r->tri_depth, 0, mvq * 32);
+	cudaMemset(r->tri_normals, 0, mvq * 8);
+	cudaMemset(r->info_block, 0, r->infoBytes());
+	err = cudaDeviceSynchronize();
+	if(err != cudaSuccess)
+		return bail(cudaFail(err, "renderer initialisation"));
+	*out = r;
+	return LUCID_OK;
+}
+
+extern "C" lucid_status lucid_destroy(lucid_renderer* r) {
+	if(!r)
+		return LUCID_OK;
+	freeAll(r);
+	delete r;
+	return LUCID_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Passes
+
+extern "C" lucid_status lucid_quad_setup(lucid_renderer* r, const lucid_frame_inputs* in, void* stream) {
+	if(!r)
+		return fail(LUCID_INVALID_ARG, "renderer is NULL");
+	lucid_status st = validateInputs(r, in);
+	if(st != LUCID_OK)
+		return st;
+	cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+	// setupInputData (src/lucid_renderer.cpp:431-451): clear LucidInfo and the bin counters
+	LUCID_CUDA_TRY(cudaMemsetAsync(r->info_block, 0, r->infoBytes(), s));
+	r->last = makeParams(r, in, nullptr);
+	r->have_frame = true;
+	launchSetup(r->last, s);
+	return checkLaunch("quad setup");
+}
+
+extern "C" lucid_status lucid_bin_count(lucid_renderer* r, void* stream) {
+	if(!r || !r->have_frame)
+		return fail(LUCID_INVALID_ARG, "lucid_bin_count needs a prior lucid_quad_setup");
+	launchBinCount(r->last, reinterpret_cast<cudaStream_t>(stream));
+	return checkLaunch("bin count");
+}
+
+extern "C" lucid_status lucid_bin_categorize(lucid_renderer* r, void* stream) {
+	if(!r || !r->have_frame)
+		return fail(LUCID_INVALID_ARG, "lucid_bin_categorize needs a prior lucid_quad_setup");
+	launchBinCategorize(r->last, reinterpret_cast<cudaStream_t>(stream));
+	return checkLaunch("bin categorize");
+}
+
+extern "C" lucid_status lucid_bin_dispatch(lucid_renderer* r, void* stream) {
+	if(!r || !r->have_frame)
+		return fail(LUCID_INVALID_ARG, "lucid_bin_dispatch needs a prior lucid_quad_setup");
+	launchBinDispatch(r->last, reinterpret_cast<cudaStream_t>(stream));
+	return checkLaunch("bin dispatch");
+}
+
+static lucid_status rasterImpl(lucid_renderer* r, const lucid_frame_inputs* in, float* out,
+							   int* dump_counts, int* dump_prims, int dump_max, cudaStream_t s) {
+	if(!r || !r->have_frame)
+		return fail(LUCID_INVALID_ARG, "lucid_raster needs a prior lucid_quad_setup");
+	if(!out)
+		return fail(LUCID_INVALID_ARG, "out_rgba is NULL");
+	lucid_status st = validateInputs(r, in);
+	if(st != LUCID_OK)
+		return st;
+	FrameParams p = r->last;
+	p.colors = in->colors;
+	p.color_format = in->color_format;
+	p.instance_colors = in->instance_colors;
+	p.tri_opacity = in->tri_opacity;
+	p.cfg.background_color[0] = in->config->background_color[0];
+	p.cfg.background_color[1] = in->config->background_color[1];
+	p.cfg.background_color[2] = in->config->background_color[2];
+	p.cfg.background_color[3] = in->config->background_color[3];
+	p.out_rgba = out;
+	p.dump_counts = dump_counts;
+	p.dump_prims = dump_prims;
+	p.dump_max = dump_max;
+	if((st = resetRasterCounters(r, s)) != LUCID_OK)
+		return st;
+	launchRaster(p, r->raster_ctas, s);
+	return checkLaunch("raster");
+}
+
+extern "C" lucid_status lucid_raster(lucid_renderer* r, const lucid_frame_inputs* in, float* out,
+									 void* stream) {
+	return rasterImpl(r, in, out, nullptr, nullptr, 0, reinterpret_cast<cudaStream_t>(stream));
+}
+
+extern "C" lucid_status lucid_render(lucid_renderer* r, const lucid_frame_inputs* in, float* out,
+									 void* stream) {
+	lucid_status st;
+	if((st = lucid_quad_setup(r, in, stream)) != LUCID_OK)
+		return st;
+	if((st = lucid_bin_count(r, stream)) != LUCID_OK)
+		return st;
+	if((st = lucid_bin_categorize(r, stream)) != LUCID_OK)
+		return st;
+	if((st = lucid_bin_dispatch(r, stream)) != LUCID_OK)
+		return st;
+	return lucid_raster(r, in, out, stream);
+}
+
+extern "C" lucid_status lucid_get_info(lucid_renderer* r, lucid_info* out, uint32_t* bin_counters,
+									   void* stream) {
+	if(!r || !out)
+		return fail(LUCID_INVALID_ARG, "lucid_get_info: bad arguments");
+	cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+	LUCID_CUDA_TRY(cudaStreamSynchronize(s));
+	LUCID_CUDA_TRY(cudaMemcpy(out, r->info_block, sizeof(lucid_info), cudaMemcpyDeviceToHost));
+	if(bin_counters)
+		LUCID_CUDA_TRY(cudaMemcpy(bin_counters, r->counts(), size_t(10) * r->bin_count * 4,
+								  cudaMemcpyDeviceToHost));
+	return LUCID_OK;
+}
+
+extern "C" lucid_status lucid_download_buffer(lucid_renderer* r, int32_t which, void* host_dst,
+											  size_t bytes, size_t* out_bytes, void* stream) {
+	if(!r)
+		return fail(LUCID_INVALID_ARG, "renderer is NULL");
+	const size_t mvq = size_t(r->opts.max_visible_quads);
+	const void* src = nullptr;
+	size_t size = 0;
+	switch(which) {
+	case LUCID_BUF_QUAD_AABBS: src = r->quad_aabbs, size = mvq * 4; break;
+	case LUCID_BUF_TRI_BARY: src = r->tri_bary, size = mvq * 64; break;
+	case LUCID_BUF_TRI_SCAN: src = r->tri_scan, size = mvq * 64; break;
+	case LUCID_BUF_TRI_DEPTH: src = r->tri_depth, size = mvq * 32; break;
+	case LUCID_BUF_QUAD_COLORS: src = r->quad_colors, size = mvq * 16; break;
+	case LUCID_BUF_TRI_NORMALS: src = r->tri_normals, size = mvq * 8; break;
+	case LUCID_BUF_QUAD_SOURCE: src = r->quad_source, size = mvq * 4; break;
+	case LUCID_BUF_BIN_QUADS: src = r->bin_quads, size = size_t(r->opts.max_bin_refs) * 4; break;
+	case LUCID_BUF_BIN_TRIS: src = r->bin_tris, size = size_t(r->opts.max_bin_refs) * 4; break;
+	case LUCID_BUF_QUAD_VERTS: src = r->quad_verts, size = mvq * 16; break;
+	default: return fail(LUCID_INVALID_ARG, "unknown buffer id");
+	}
+	if(out_bytes)
+		*out_bytes = size;
+	if(host_dst && bytes) {
+		LUCID_CUDA_TRY(cudaStreamSynchronize(reinterpret_cast<cudaStream_t>(stream)));
+		LUCID_CUDA_TRY(cudaMemcpy(host_dst, src, std::min(bytes, size), cudaMemcpyDeviceToHost));
+	}
+	return LUCID_OK;
+}
+
+extern "C" lucid_status lucid_raster_dump(lucid_renderer* r, const lucid_frame_inputs* in, float* out,
+										  int32_t max_per_pixel, int32_t* host_counts,
+										  int32_t* host_prims, void* stream) {
+	if(!r || !host_counts || max_per_pixel < 0 || (max_per_pixel > 0 && !host_prims))
+		return fail(LUCID_INVALID_ARG, "lucid_raster_dump: bad arguments");
+	cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+	const size_t npix = size_t(r->width) * r->height;
+	int *dc = nullptr, *dp = nullptr;
+	LUCID_CUDA_TRY(cudaMalloc(&dc, npix * 4));
+	if(max_per_pixel > 0) {
+		cudaError_t err = cudaMalloc(&dp, npix * max_per_pixel * 4);
+		if(err != cudaSuccess) {
+			cudaFree(dc);
+			return cudaFail(err, "cudaMalloc(dump)");
+		}
+		cudaMemsetAsync(dp, 0xff, npix * max_per_pixel * 4, s);
+	}
+	cudaMemsetAsync(dc, 0, npix * 4, s);
+	lucid_status st = lucid_quad_setup(r, in, stream);
+	if(st == LUCID_OK)
+		st = lucid_bin_count(r, stream);
+	if(st == LUCID_OK)
+		st = lucid_bin_categorize(r, stream);
+	if(st == LUCID_OK)
+		st = lucid_bin_dispatch(r, stream);
+	if(st == LUCID_OK)
+		st = rasterImpl(r, in, out, dc, dp, max_per_pixel, s);
+	if(st == LUCID_OK) {
+		cudaError_t err = cudaStreamSynchronize(s);
+		if(err == cudaSuccess)
+			err = cudaMemcpy(host_counts, dc, npix * 4, cudaMemcpyDeviceToHost);
+		if(err == cudaSuccess && dp)
+			err = cudaMemcpy(host_prims, dp, npix * max_per_pixel * 4, cudaMemcpyDeviceToHost);
+		if(err != cudaSuccess)
+			st = cudaFail(err, "lucid_raster_dump readback");
+	}
+	cudaFree(dc);
+	if(dp)
+		cudaFree(dp);
+	return st;
+}
+
+extern "C" lucid_status lucid_render_backward(lucid_renderer* r, const lucid_frame_inputs* in,
+											  const float* dl_dimage, float* dvertex_rgba,
+											  float* dtri_opacity, void* stream) {
+	(void)r, (void)in, (void)dl_dimage, (void)dvertex_rgba, (void)dtri_opacity, (void)stream;
+	return fail(LUCID_NOT_SUPPORTED, "lucid_render_backward is not built yet");
+}
+
+extern "C" lucid_status lucid_render_batch(lucid_renderer* r, const lucid_view* views,
+										   int32_t num_views, void* stream) {
+	(void)r, (void)views, (void)num_views, (void)stream;
+	return fail(LUCID_NOT_SUPPORTED, "lucid_render_batch is not built yet");
+}
+
+extern "C" lucid_status lucid_autotune(lucid_renderer* r, const lucid_frame_inputs* in,
+									   float* scratch_rgba, int32_t* out_ctas_per_sm,
+									   int32_t* out_low_high_threshold, void* stream) {
+	(void)r, (void)in, (void)scratch_rgba, (void)out_ctas_per_sm, (void)out_low_high_threshold,
+		(void)stream;
+	return fail(LUCID_NOT_SUPPORTED, "lucid_autotune is not built yet");
+}

@@ -1,0 +1,140 @@
+"""ctypes binding of the CPU oracle (test infrastructure only).
+
+``run(scene, ...)`` executes quad setup, binning and (optionally) the exact raster pass on the
+CPU and returns every intermediate as numpy arrays in the same layout the CUDA path uses.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+
+
+class OracleInputs(ctypes.Structure):
+    _fields_ = [
+        ("width", ctypes.c_int32), ("height", ctypes.c_int32),
+        ("max_visible_quads", ctypes.c_int32), ("low_high_threshold", ctypes.c_int32),
+        ("flags", ctypes.c_uint32), ("order_mode", ctypes.c_int32),
+        ("positions", ctypes.c_void_p), ("colors", ctypes.c_void_p),
+        ("color_format", ctypes.c_int32), ("num_verts", ctypes.c_int32),
+        ("quads_ib", ctypes.c_void_p), ("num_quads", ctypes.c_int32),
+        ("num_instances", ctypes.c_int32), ("instances", ctypes.c_void_p),
+        ("instance_colors", ctypes.c_void_p), ("tri_opacity", ctypes.c_void_p),
+        ("config", ctypes.c_void_p),
+        ("bin_subset", ctypes.c_void_p), ("num_bin_subset", ctypes.c_int32),
+        ("num_threads", ctypes.c_int32),
+    ]
+
+
+class OracleOutputs(ctypes.Structure):
+    _fields_ = [
+        ("num_input_quads", ctypes.c_int32), ("num_visible", ctypes.c_int32 * 2),
+        ("rejected", ctypes.c_uint32 * 4), ("error_code", ctypes.c_uint32),
+        ("num_binning_dispatches", ctypes.c_uint32),
+        ("quad_aabbs", ctypes.c_void_p), ("quad_source", ctypes.c_void_p),
+        ("quad_colors", ctypes.c_void_p), ("quad_verts", ctypes.c_void_p),
+        ("tri_bary", ctypes.c_void_p), ("tri_scan", ctypes.c_void_p),
+        ("tri_depth", ctypes.c_void_p), ("tri_normals", ctypes.c_void_p),
+        ("bin_count", ctypes.c_int32), ("bin_count_x", ctypes.c_int32),
+        ("bin_count_y", ctypes.c_int32),
+        ("bin_counters", ctypes.c_void_p), ("bin_quads", ctypes.c_void_p),
+        ("bin_tris", ctypes.c_void_p), ("bin_refs_capacity", ctypes.c_int64),
+        ("num_bin_quads", ctypes.c_int64), ("num_bin_tris", ctypes.c_int64),
+        ("bin_level_counts", ctypes.c_int32 * 5),
+        ("image", ctypes.c_void_p), ("image64", ctypes.c_void_p),
+        ("frag_counts", ctypes.c_void_p), ("frag_prims", ctypes.c_void_p),
+        ("max_per_pixel", ctypes.c_int32),
+        ("num_fragments", ctypes.c_uint64), ("num_hblock_tris", ctypes.c_uint64),
+        ("max_pixel_fragments", ctypes.c_uint32), ("invalid_pixels", ctypes.c_uint64),
+    ]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        _lib = ctypes.CDLL(path)
+        _lib.oracle_run.argtypes = [ctypes.POINTER(OracleInputs), ctypes.POINTER(OracleOutputs)]
+        _lib.oracle_run.restype = ctypes.c_int
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+def run(scene, max_visible_quads: int | None = None, raster: bool = True, image64: bool = False,
+        bin_subset=None, threads: int = 1, max_per_pixel: int = 0, flags: int = 0,
+        low_high_threshold: int = 1024, setup_outputs: bool = True):
+    """Runs the oracle on a ``lucid_gb300.scenes.Scene``; returns a dict of numpy arrays."""
+    L = lib()
+    mvq = max_visible_quads or max(1024, scene.num_quads)
+    w, h = scene.width, scene.height
+    positions = np.ascontiguousarray(scene.positions, dtype=np.float32)
+    colors = np.ascontiguousarray(scene.colors)
+    quads = np.ascontiguousarray(scene.quads, dtype=np.uint32)
+    inst = np.ascontiguousarray(scene.instances, dtype=np.int32)
+    icol = np.ascontiguousarray(scene.instance_colors, dtype=np.uint32)
+    opac = None if scene.tri_opacity is None else np.ascontiguousarray(scene.tri_opacity, np.float32)
+    subset = None if bin_subset is None else np.ascontiguousarray(np.sort(bin_subset), np.int32)
+
+    bins_x, bins_y = (w + 31) // 32, (h + 31) // 32
+    bins = bins_x * bins_y
+    out = {}
+    if setup_outputs:
+        out["quad_aabbs"] = np.zeros(mvq, np.uint32)
+        out["quad_source"] = np.zeros(mvq, np.uint32)
+        out["quad_colors"] = np.zeros((mvq, 4), np.uint32)
+        out["quad_verts"] = np.zeros((mvq, 4), np.uint32)
+        out["tri_bary"] = np.zeros((2 * mvq, 8), np.uint32)
+        out["tri_scan"] = np.zeros((2 * mvq, 8), np.uint32)
+        out["tri_depth"] = np.zeros((2 * mvq, 4), np.uint32)
+        out["tri_normals"] = np.zeros(2 * mvq, np.uint32)
+    out["bin_counters"] = np.zeros(10 * bins, np.uint32)
+    cap = int(8 * scene.num_quads + 1024)
+    out["bin_quads"] = np.zeros(cap, np.uint32)
+    out["bin_tris"] = np.zeros(cap, np.uint32)
+    if raster:
+        out["image"] = np.zeros((h, w, 4), np.float32)
+        out["frag_counts"] = np.zeros((h, w), np.int32)
+        if image64:
+            out["image64"] = np.zeros((h, w, 4), np.float64)
+        if max_per_pixel > 0:
+            out["frag_prims"] = np.full((h, w, max_per_pixel), -1, np.int32)
+
+    cfg = scene.config
+    ins = OracleInputs(
+        width=w, height=h, max_visible_quads=mvq, low_high_threshold=low_high_threshold,
+        flags=flags, order_mode=0, positions=_ptr(positions), colors=_ptr(colors),
+        color_format=scene.color_format, num_verts=positions.shape[0], quads_ib=_ptr(quads),
+        num_quads=quads.shape[0], num_instances=inst.shape[0], instances=_ptr(inst),
+        instance_colors=_ptr(icol), tri_opacity=_ptr(opac), config=ctypes.addressof(cfg),
+        bin_subset=_ptr(subset), num_bin_subset=0 if subset is None else len(subset),
+        num_threads=max(1, threads))
+    outs = OracleOutputs()
+    for k, v in out.items():
+        setattr(outs, k, v.ctypes.data)
+    outs.bin_refs_capacity = cap
+    outs.max_per_pixel = max_per_pixel
+    rc = L.oracle_run(ctypes.byref(ins), ctypes.byref(outs))
+    if rc != 0:
+        raise RuntimeError(f"oracle_run failed ({rc})")
+    nbq, nbt = int(outs.num_bin_quads), int(outs.num_bin_tris)
+    if nbq > cap or nbt > cap:
+        raise RuntimeError("oracle bin reference capacity exceeded")
+    out["bin_quads"] = out["bin_quads"][:nbq]
+    out["bin_tris"] = out["bin_tris"][:nbt]
+    out.update(
+        num_input_quads=outs.num_input_quads, num_visible=tuple(outs.num_visible),
+        rejected=tuple(outs.rejected), error_code=outs.error_code,
+        num_binning_dispatches=outs.num_binning_dispatches,
+        bin_count=outs.bin_count, bin_count_x=outs.bin_count_x, bin_count_y=outs.bin_count_y,
+        bin_level_counts=tuple(outs.bin_level_counts), num_fragments=int(outs.num_fragments),
+        num_hblock_tris=int(outs.num_hblock_tris),
+        max_pixel_fragments=int(outs.max_pixel_fragments), max_visible_quads=mvq)
+    return out

@@ -1,0 +1,874 @@
+// Scalar CPU oracle of LucidRaster's compute rasterization path (test infrastructure only).
+//
+// Each function restates one piece of the reference shaders (paths relative to the
+// LucidRaster source tree) in plain single-threaded C++ with IEEE float arithmetic, no FMA
+// contraction (built with -ffp-contract=off) and the float->int conversion rules of the GPU
+// (saturating, NaN -> 0). Bin lists are produced in canonical order (per bin, by slot).
+//
+// Parity with the reference is unpinned (no runnable reference, no golden vectors); see the
+// header for what pins it instead.
+
+#include "lucid_oracle.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+namespace {
+
+// ---------------------------------------------------------------------------------------------
+// Arithmetic helpers with explicit evaluation order
+
+struct V3 {
+	float x, y, z;
+};
+struct V4 {
+	float x, y, z, w;
+};
+
+inline V3 v3(float x, float y, float z) { return V3{x, y, z}; }
+inline V3 sub(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline V3 add(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+inline V3 mul(V3 a, float s) { return v3(a.x * s, a.y * s, a.z * s); }
+inline bool eq(V3 a, V3 b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
+// GLSL dot/cross evaluated left to right
+inline float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline V3 cross(V3 a, V3 b) {
+	return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+inline V3 xyz(const float* v) { return v3(v[0], v[1], v[2]); }
+
+// GLSL int(float): truncation; saturating with NaN -> 0 (PTX cvt.rzi.s32.f32 semantics)
+inline int f2i(float x) {
+	if(x != x)
+		return 0;
+	if(x >= 2147483648.0f)
+		return 2147483647;
+	if(x <= -2147483648.0f)
+		return (-2147483647 - 1);
+	return (int)x;
+}
+inline uint32_t f2u(float x) {
+	if(x != x || x <= 0.0f)
+		return 0u;
+	if(x >= 4294967296.0f)
+		return 0xffffffffu;
+	return (uint32_t)x;
+}
+inline uint32_t fbits(float f) {
+	uint32_t u;
+	memcpy(&u, &f, 4);
+	return u;
+}
+inline float bitsf(uint32_t u) {
+	float f;
+	memcpy(&f, &u, 4);
+	return f;
+}
+// Ascending key of "nearest first": larger inv_ray_pos sorts first.
+inline uint32_t nearFirstKey(float inv_ray_pos) {
+	uint32_t u = fbits(inv_ray_pos);
+	uint32_t asc = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+	return ~asc;
+}
+
+// mat4 (column-major) * vec4(p, 1): ((c0*x + c1*y) + c2*z) + c3
+inline V4 mulPoint(const float* m, V3 p) {
+	V4 r;
+	r.x = m[0] * p.x + m[4] * p.y + m[8] * p.z + m[12];
+	r.y = m[1] * p.x + m[5] * p.y + m[9] * p.z + m[13];
+	r.z = m[2] * p.x + m[6] * p.y + m[10] * p.z + m[14];
+	r.w = m[3] * p.x + m[7] * p.y + m[11] * p.z + m[15];
+	return r;
+}
+
+// funcs.glsl:52-59
+inline uint32_t encodeAABB28(uint32_t x0, uint32_t y0, uint32_t x1, uint32_t y1) {
+	return (x0 & 0x7fu) | ((y0 & 0x7fu) << 7) | ((x1 & 0x7fu) << 14) | ((y1 & 0x7fu) << 21);
+}
+inline void decodeAABB28(uint32_t a, int& x0, int& y0, int& x1, int& y1) {
+	x0 = int(a & 0x7fu), y0 = int((a >> 7) & 0x7fu), x1 = int((a >> 14) & 0x7fu),
+	y1 = int((a >> 21) & 0x7fu);
+}
+// funcs.glsl:28-33
+inline uint32_t encodeNormalUint(V3 n) {
+	uint32_t x = f2u(512.0f + n.x * 511.0f) & 0x3ffu;
+	uint32_t y = f2u(512.0f + n.y * 511.0f) & 0x3ffu;
+	uint32_t z = f2u(512.0f + n.z * 511.0f) & 0x3ffu;
+	return x | (y << 10) | (z << 20);
+}
+// funcs.glsl:100-104
+inline void decodeRGBA8(uint32_t c, float out[4]) {
+	const float s = 1.0f / 255.0f;
+	out[0] = float(c & 0xffu) * s;
+	out[1] = float((c >> 8) & 0xffu) * s;
+	out[2] = float((c >> 16) & 0xffu) * s;
+	out[3] = float((c >> 24) & 0xffu) * s;
+}
+inline float halfToFloat(uint16_t h) {
+	uint32_t sign = uint32_t(h >> 15) << 31;
+	uint32_t exp = (h >> 10) & 0x1f, man = h & 0x3ff;
+	uint32_t bits;
+	if(exp == 0) {
+		if(man == 0)
+			bits = sign;
+		else { // subnormal half -> normal float
+			int e = -1;
+			do {
+				man <<= 1;
+				e++;
+			} while(!(man & 0x400));
+			man &= 0x3ff;
+			bits = sign | (uint32_t(127 - 15 - e) << 23) | (man << 13);
+		}
+	} else if(exp == 31)
+		bits = sign | 0x7f800000u | (man << 13);
+	else
+		bits = sign | ((exp + 112) << 23) | (man << 13);
+	return bitsf(bits);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Pass state
+
+constexpr int kBinSize = 32, kBinShift = 5;
+constexpr int kMaxDispatches = 256;
+
+struct QuadResult {
+	int cls = -1; // -1 rejected, 0 small, 1 large
+	int reason = 0;
+	uint32_t enc_aabb = 0, y_aabb[2] = {0, 0};
+	uint32_t v[4] = {0, 0, 0, 0};
+	bool bad_index = false;
+};
+
+struct State {
+	const oracle_inputs* in;
+	int w, h, bcx, bcy, bins, mvq;
+	V3 origin, dir0, dirx, diry, ray_dir0;
+	// outputs of setup
+	std::vector<uint32_t> quad_aabbs, quad_source, quad_colors, quad_verts;
+	std::vector<uint32_t> tri_bary, tri_scan, tri_depth, tri_normals;
+	std::vector<uint32_t> quad_inst; // instance id per quad slot
+	int nvis[2] = {0, 0};
+	// binning
+	std::vector<std::vector<uint32_t>> bin_quads, bin_tris;
+};
+
+V3 vertexLoad(const State& s, uint32_t idx) {
+	const float* p = s.in->positions + size_t(idx) * 3;
+	return v3(p[0], p[1], p[2]);
+}
+
+// quad_setup.glsl:68-72
+uint32_t vertexClipMask(V4 p) {
+	return (p.x < -p.w ? 0x001u : 0u) | (p.x > p.w ? 0x002u : 0u) | (p.y < -p.w ? 0x004u : 0u) |
+		   (p.y > p.w ? 0x008u : 0u) | (p.z < -p.w ? 0x010u : 0u) | (p.z > p.w ? 0x020u : 0u);
+}
+
+// quad_setup.glsl:77-128 (Blinn's clipped screen coverage)
+void computeClippedAABB(const V4 vn[3], const float inv_w[3], uint32_t clipmask, float aabb[4]) {
+	aabb[0] = 1.0f, aabb[1] = 1.0f, aabb[2] = -1.0f, aabb[3] = -1.0f;
+	int any_vis = 0;
+	uint32_t or_clipmask = clipmask | (clipmask >> 8) | (clipmask >> 16);
+	for(int i = 0; i < 3; i++) {
+		uint32_t cur = clipmask >> (i * 8);
+		if((cur & 0x3u) == 0) {
+			any_vis |= 0x1;
+			if(vn[i].x - aabb[0] * vn[i].w < 0.0f)
+				aabb[0] = vn[i].x * inv_w[i];
+			if(vn[i].x - aabb[2] * vn[i].w > 0.0f)
+				aabb[2] = vn[i].x * inv_w[i];
+		}
+		if((cur & 0xcu) == 0) {
+			any_vis |= 0x10;
+			if(vn[i].y - aabb[1] * vn[i].w < 0.0f)
+				aabb[1] = vn[i].y * inv_w[i];
+			if(vn[i].y - aabb[3] * vn[i].w > 0.0f)
+				aabb[3] = vn[i].y * inv_w[i];
+		}
+	}
+	if((any_vis & 0x0f) == 0) {
+		aabb[0] = -1.0f, aabb[2] = 1.0f;
+	} else if((or_clipmask & 0x3u) != 0) {
+		for(int i = 0; i < 3; i++) {
+			uint32_t cur = clipmask >> (i * 8);
+			if((cur & 0x1u) != 0 && vn[i].x - aabb[0] * vn[i].w < 0.0f)
+				aabb[0] = -1.0f;
+			if((cur & 0x2u) != 0 && vn[i].x - aabb[2] * vn[i].w > 0.0f)
+				aabb[2] = 1.0f;
+		}
+	}
+	if((any_vis & 0xf0) == 0) {
+		aabb[1] = -1.0f, aabb[3] = 1.0f;
+	} else if((or_clipmask & 0xcu) != 0) {
+		for(int i = 0; i < 3; i++) {
+			uint32_t cur = clipmask >> (i * 8);
+			if((cur & 0x4u) != 0 && vn[i].y - aabb[1] * vn[i].w < 0.0f)
+				aabb[1] = -1.0f;
+			if((cur & 0x8u) != 0 && vn[i].y - aabb[3] * vn[i].w > 0.0f)
+				aabb[3] = 1.0f;
+		}
+	}
+}
+
+// quad_setup.glsl:136-254 (processInputQuad): cull tests, clipped AABB, bin AABB, class.
+QuadResult processInputQuad(const State& s, const uint32_t v[4]) {
+	QuadResult r;
+	for(int i = 0; i < 4; i++)
+		r.v[i] = v[i];
+	const lucid_config& cfg = *s.in->config;
+	bool cull0 = v[0] == v[1] || v[1] == v[2] || v[2] == v[0];
+	bool cull1 = v[0] == v[2] || v[2] == v[3] || v[3] == v[0];
+	if(cull0 && cull1) {
+		r.reason = LUCID_REJECTION_TYPE_OTHER;
+		return r;
+	}
+	uint32_t nv = uint32_t(s.in->num_verts);
+	if(v[0] >= nv || v[1] >= nv || v[2] >= nv || v[3] >= nv) {
+		r.reason = LUCID_REJECTION_TYPE_OTHER;
+		r.bad_index = true;
+		return r;
+	}
+	V3 vws[4] = {vertexLoad(s, v[0]), vertexLoad(s, v[1]), vertexLoad(s, v[2]),
+				 vertexLoad(s, v[3])};
+	cull0 = cull0 || eq(vws[0], vws[1]) || eq(vws[1], vws[2]) || eq(vws[2], vws[0]);
+	cull1 = cull1 || eq(vws[0], vws[2]) || eq(vws[2], vws[3]) || eq(vws[3], vws[0]);
+
+	if(cfg.enable_backface_culling != 0) {
+		V3 o = s.origin;
+		V3 p0 = sub(vws[0], o), p1 = sub(vws[1], o), p2 = sub(vws[2], o), p3 = sub(vws[3], o);
+		V3 nrm0 = cross(p2, sub(p1, p2));
+		V3 nrm1 = cross(p3, sub(p2, p3));
+		float volume0 = dot(p0, nrm0);
+		float volume1 = dot(p0, nrm1);
+		cull0 = cull0 || volume0 <= 0.0f;
+		cull1 = cull1 || volume1 <= 0.0f;
+		if(cull0 && cull1) {
+			r.reason = LUCID_REJECTION_TYPE_BACKFACE;
+			return r;
+		}
+	}
+	uint32_t cull_flags = (cull0 ? 1u : 0u) | (cull1 ? 2u : 0u);
+
+	V4 vndc[4];
+	for(int i = 0; i < 4; i++)
+		vndc[i] = mulPoint(cfg.view_proj_matrix, vws[i]);
+	uint32_t clipmask = vertexClipMask(vndc[0]) | (vertexClipMask(vndc[1]) << 8) |
+						(vertexClipMask(vndc[2]) << 16) | (vertexClipMask(vndc[3]) << 24);
+	uint32_t and_clipmask =
+		clipmask & (clipmask >> 8) & (clipmask >> 16) & (clipmask >> 24) & 0xffu;
+	uint32_t or_clipmask = clipmask | (clipmask >> 8) | (clipmask >> 16) | (clipmask >> 24);
+	if(and_clipmask != 0) {
+		r.reason = LUCID_REJECTION_TYPE_FRUSTUM;
+		return r;
+	}
+
+	float aabb0[4], aabb1[4];
+	float inv_w[4] = {1.0f / vndc[0].w, 1.0f / vndc[1].w, 1.0f / vndc[2].w, 1.0f / vndc[3].w};
+	if((or_clipmask & 0x30u) != 0) {
+		V4 t0[3] = {vndc[0], vndc[1], vndc[2]};
+		float iw0[3] = {inv_w[0], inv_w[1], inv_w[2]};
+		computeClippedAABB(t0, iw0, clipmask, aabb0);
+		V4 t1[3] = {vndc[0], vndc[2], vndc[3]};
+		float iw1[3] = {inv_w[0], inv_w[2], inv_w[3]};
+		computeClippedAABB(t1, iw1, (clipmask & 0xffu) | ((clipmask & 0xffff0000u) >> 8), aabb1);
+	}
+	for(int i = 0; i < 4; i++) {
+		vndc[i].x *= inv_w[i];
+		vndc[i].y *= inv_w[i];
+		vndc[i].z *= inv_w[i];
+	}
+	if((or_clipmask & 0x30u) == 0) {
+		// computeAABB (quad_setup.glsl:131-134); min/max ignore NaN on both CPU and GPU
+		aabb0[0] = fminf(fminf(vndc[0].x, vndc[1].x), vndc[2].x);
+		aabb0[1] = fminf(fminf(vndc[0].y, vndc[1].y), vndc[2].y);
+		aabb0[2] = fmaxf(fmaxf(vndc[0].x, vndc[1].x), vndc[2].x);
+		aabb0[3] = fmaxf(fmaxf(vndc[0].y, vndc[1].y), vndc[2].y);
+		aabb1[0] = fminf(fminf(vndc[0].x, vndc[2].x), vndc[3].x);
+		aabb1[1] = fminf(fminf(vndc[0].y, vndc[2].y), vndc[3].y);
+		aabb1[2] = fmaxf(fmaxf(vndc[0].x, vndc[2].x), vndc[3].x);
+		aabb1[3] = fmaxf(fmaxf(vndc[0].y, vndc[2].y), vndc[3].y);
+	}
+
+	const float hx = float(s.w) * 0.5f, hy = float(s.h) * 0.5f;
+	const float mx = float(s.w - 1), my = float(s.h - 1);
+	float scale[4] = {hx, hy, hx, hy};
+	for(int i = 0; i < 4; i++) {
+		aabb0[i] = (aabb0[i] + 1.0f) * scale[i];
+		aabb1[i] = (aabb1[i] + 1.0f) * scale[i];
+	}
+	float aabb[4] = {fminf(aabb0[0], aabb1[0]), fminf(aabb0[1], aabb1[1]),
+					 fmaxf(aabb0[2], aabb1[2]), fmaxf(aabb0[3], aabb1[3])};
+
+	// quad_setup.glsl:227-231 (quads falling between samples)
+	if(ceilf(aabb[0] - 0.5001f) == floorf(aabb[2] + 0.5001f) ||
+	   ceilf(aabb[1] - 0.5001f) == floorf(aabb[3] + 0.5001f)) {
+		r.reason = LUCID_REJECTION_TYPE_BETWEEN_SAMPLES;
+		return r;
+	}
+
+	const float adj[4] = {0.49f, 0.49f, -0.49f, -0.49f};
+	const float hi[4] = {mx, my, mx, my};
+	for(int i = 0; i < 4; i++) {
+		aabb0[i] = fminf(fmaxf(aabb0[i] + adj[i], 0.0f), hi[i]);
+		aabb1[i] = fminf(fmaxf(aabb1[i] + adj[i], 0.0f), hi[i]);
+		aabb[i] = fminf(fmaxf(aabb[i] + adj[i], 0.0f), hi[i]);
+	}
+	uint32_t b[4];
+	for(int i = 0; i < 4; i++)
+		b[i] = f2u(aabb[i]) >> kBinShift;
+	r.enc_aabb = encodeAABB28(b[0], b[1], b[2], b[3]) | (cull_flags << 30);
+	uint32_t bw = b[2] - b[0] + 1, bh = b[3] - b[1] + 1;
+	r.cls = bw * bh <= 4 ? 0 : 1;
+	r.y_aabb[0] = f2u(aabb0[1]) | (f2u(aabb0[3]) << 16);
+	r.y_aabb[1] = f2u(aabb1[1]) | (f2u(aabb1[3]) << 16);
+	return r;
+}
+
+// quad_setup.glsl:274-340 (storeTri)
+void storeTri(State& s, uint32_t tri_idx, uint32_t inst_flags_id, V3 tri0, V3 tri1, V3 tri2,
+			  uint32_t y_aabb) {
+	V3 normal = cross(sub(tri0, tri2), sub(tri1, tri0));
+	float multiplier = 1.0f / sqrtf(dot(normal, normal));
+	normal = mul(normal, multiplier);
+	if((inst_flags_id & LUCID_INST_HAS_VERTEX_NORMALS) == 0)
+		s.tri_normals[tri_idx] = encodeNormalUint(normal);
+
+	V3 edge0 = mul(sub(tri0, tri2), multiplier);
+	V3 edge1 = mul(sub(tri1, tri0), multiplier);
+	float plane_dist = dot(normal, tri0);
+	V3 nrm_tri0 = cross(tri0, normal);
+	float param0 = dot(edge0, nrm_tri0);
+	float param1 = dot(edge1, nrm_tri0);
+	edge0 = cross(normal, edge0);
+	edge1 = cross(normal, edge1);
+	V3 e0 = v3(dot(edge0, s.dirx), dot(edge0, s.diry), dot(edge0, s.ray_dir0));
+	V3 e1 = v3(dot(edge1, s.dirx), dot(edge1, s.diry), dot(edge1, s.ray_dir0));
+	V3 pnormal = mul(normal, 1.0f / plane_dist);
+	V3 deq = v3(dot(pnormal, s.dirx), dot(pnormal, s.diry), dot(pnormal, s.ray_dir0));
+
+	uint32_t* d = &s.tri_depth[size_t(tri_idx) * 4];
+	d[0] = fbits(deq.x), d[1] = fbits(deq.y), d[2] = fbits(deq.z), d[3] = inst_flags_id;
+	uint32_t* bary = &s.tri_bary[size_t(tri_idx) * 8];
+	bary[0] = fbits(e0.x), bary[1] = fbits(e0.y), bary[2] = fbits(e0.z), bary[3] = fbits(param0);
+	bary[4] = fbits(e1.x), bary[5] = fbits(e1.y), bary[6] = fbits(e1.z), bary[7] = fbits(param1);
+
+	V3 nrm0 = cross(tri2, sub(tri1, tri2));
+	V3 nrm1 = cross(tri0, sub(tri2, tri0));
+	V3 nrm2 = cross(tri1, sub(tri0, tri1));
+	float volume = dot(tri0, nrm0);
+	if(volume < 0.0f) {
+		nrm0 = v3(-nrm0.x, -nrm0.y, -nrm0.z);
+		nrm1 = v3(-nrm1.x, -nrm1.y, -nrm1.z);
+		nrm2 = v3(-nrm2.x, -nrm2.y, -nrm2.z);
+	}
+	V3 edges[3] = {v3(dot(nrm0, s.dirx), dot(nrm0, s.diry), dot(nrm0, s.dir0)),
+				   v3(dot(nrm1, s.dirx), dot(nrm1, s.diry), dot(nrm1, s.dir0)),
+				   v3(dot(nrm2, s.dirx), dot(nrm2, s.diry), dot(nrm2, s.dir0))};
+	float scan[3], step[3];
+	uint32_t signs = 0;
+	for(int i = 0; i < 3; i++) {
+		float inv_ex = 1.0f / edges[i].x;
+		float base = -(edges[i].z * inv_ex);
+		step[i] = -(edges[i].y * inv_ex);
+		// scan = scan_step * 0.5 + scan_base - (-0.5)
+		scan[i] = (step[i] * 0.5f + base) - (-0.5f);
+		signs |= (edges[i].x < 0.0f ? (1u << i) : 0u) | (edges[i].y < 0.0f ? (8u << i) : 0u);
+	}
+	uint32_t* sc = &s.tri_scan[size_t(tri_idx) * 8];
+	sc[0] = fbits(scan[0]), sc[1] = fbits(scan[1]), sc[2] = fbits(scan[2]), sc[3] = y_aabb;
+	sc[4] = fbits(step[0]), sc[5] = fbits(step[1]), sc[6] = fbits(step[2]), sc[7] = signs;
+}
+
+// quad_setup.glsl:374-489 with deterministic slot assignment in input order.
+void quadSetup(State& s, oracle_outputs* out) {
+	const oracle_inputs* in = s.in;
+	int mvq = s.mvq;
+	s.quad_aabbs.assign(mvq, 0);
+	s.quad_source.assign(mvq, 0);
+	s.quad_colors.assign(size_t(mvq) * 4, 0);
+	s.quad_verts.assign(size_t(mvq) * 4, 0);
+	s.quad_inst.assign(mvq, 0);
+	s.tri_bary.assign(size_t(mvq) * 16, 0);
+	s.tri_scan.assign(size_t(mvq) * 16, 0);
+	s.tri_depth.assign(size_t(mvq) * 8, 0);
+	s.tri_normals.assign(size_t(mvq) * 2, 0);
+	int num_small = 0, num_large = 0;
+	uint32_t rejected[4] = {0, 0, 0, 0};
+	uint32_t input_quad = 0;
+	for(int inst = 0; inst < in->num_instances; inst++) {
+		const lucid_instance& id = in->instances[inst];
+		if(id.num_quads > LUCID_MAX_INSTANCE_QUADS && out->error_code == 0)
+			out->error_code = LUCID_ERR_INSTANCE_QUADS;
+		for(int lq = 0; lq < id.num_quads; lq++, input_quad++) {
+			size_t io = size_t(id.index_offset) + size_t(lq) * 4;
+			uint32_t v[4];
+			for(int k = 0; k < 4; k++)
+				v[k] = in->quads_ib[io + k] + uint32_t(id.vertex_offset);
+			QuadResult r = processInputQuad(s, v);
+			if(r.cls < 0) {
+				rejected[r.reason]++;
+				if(r.bad_index && out->error_code == 0)
+					out->error_code = LUCID_ERR_VERTEX_INDEX;
+				continue;
+			}
+			if(num_small + num_large >= mvq) {
+				if(out->error_code == 0)
+					out->error_code = LUCID_ERR_VISIBLE_QUADS;
+				continue;
+			}
+			int slot = r.cls == 0 ? num_small++ : (mvq - 1) - num_large++;
+			s.quad_aabbs[slot] = r.enc_aabb;
+			s.quad_source[slot] = input_quad;
+			s.quad_inst[slot] = uint32_t(inst);
+			for(int k = 0; k < 4; k++)
+				s.quad_verts[size_t(slot) * 4 + k] = v[k];
+			uint32_t flags = id.flags;
+			// storeQuad (quad_setup.glsl:256-272): RGBA8 vertex colours
+			if((flags & LUCID_INST_HAS_VERTEX_COLORS) && in->color_format == LUCID_COLOR_RGBA8) {
+				const uint32_t* cols = (const uint32_t*)in->colors;
+				for(int k = 0; k < 4; k++)
+					s.quad_colors[size_t(slot) * 4 + k] = cols[v[k]];
+			}
+			uint32_t inst_flags_id = (flags & 0xffffu) | (uint32_t(inst) << 16);
+			for(int second = 0; second < 2; second++) {
+				// addVisibleTri (quad_setup.glsl:356-372)
+				if((r.enc_aabb >> (30 + second)) & 1u)
+					continue;
+				V3 t0 = sub(vertexLoad(s, v[0]), s.origin);
+				V3 t1 = sub(vertexLoad(s, v[1 + second]), s.origin);
+				V3 t2 = sub(vertexLoad(s, v[2 + second]), s.origin);
+				storeTri(s, uint32_t(slot) * 2 + second, inst_flags_id, t0, t1, t2,
+						 r.y_aabb[second]);
+			}
+		}
+	}
+	s.nvis[0] = num_small, s.nvis[1] = num_large;
+	out->num_input_quads = int32_t(input_quad);
+	out->num_visible[0] = num_small, out->num_visible[1] = num_large;
+	for(int i = 0; i < 4; i++)
+		out->rejected[i] = rejected[i];
+	// quad_setup.glsl:471-485 (binning dispatch size)
+	int small_batch = 1024 * 4, large_batch = 1024 / 2;
+	int tasks = (num_small + small_batch - 1) / small_batch + (num_large + large_batch - 1) / large_batch;
+	out->num_binning_dispatches = uint32_t(std::min(std::max(tasks, 4), kMaxDispatches));
+}
+
+// ---------------------------------------------------------------------------------------------
+// Binning: bin_counter.glsl, bin_categorizer.glsl, bin_dispatcher.glsl
+
+struct BinScan {
+	float mn[3], mx[3], step[3];
+};
+
+// scanline.glsl:28-52 (loadScanlineParamsBin)
+BinScan loadScanlineParamsBin(const uint32_t* sc, int& min_by, int& max_by) {
+	BinScan p;
+	float scan[3] = {bitsf(sc[0]), bitsf(sc[1]), bitsf(sc[2])};
+	for(int i = 0; i < 3; i++)
+		p.step[i] = bitsf(sc[4 + i]);
+	min_by = int(sc[3] & 0xffffu) >> kBinShift;
+	max_by = int(sc[3] >> 16) >> kBinShift;
+	uint32_t sg = sc[7];
+	const float offset = float(kBinSize) - 0.989f;
+	const float start_x = 0.99f, start_y = float(min_by * kBinSize) - 0.01f;
+	const float inf = INFINITY;
+	for(int i = 0; i < 3; i++) {
+		bool xneg = (sg >> i) & 1u, yneg = (sg >> (3 + i)) & 1u;
+		float yoff = yneg ? 0.0f : offset, xoff = xneg ? 0.0f : offset;
+		// scan += step * (yoffset + start.y) - (xoffset + start.x)
+		scan[i] = scan[i] + (p.step[i] * (yoff + start_y) - (xoff + start_x));
+		p.mn[i] = xneg ? -inf : scan[i];
+		p.mx[i] = xneg ? scan[i] : inf;
+		p.step[i] = p.step[i] * float(kBinSize);
+	}
+	return p;
+}
+
+// bin_counter.glsl:53-62 (scanlineStep)
+void scanlineStep(BinScan& p, int& bmin, int& bmax) {
+	float xmin = fmaxf(fmaxf(p.mn[0], p.mn[1]), p.mn[2]);
+	float xmax = fminf(fminf(p.mx[0], p.mx[1]), p.mx[2]);
+	for(int i = 0; i < 3; i++)
+		p.mn[i] += p.step[i], p.mx[i] += p.step[i];
+	bmin = f2i(xmin + 1.0f) >> kBinShift;
+	bmax = f2i(xmax) >> kBinShift;
+}
+
+void binning(State& s, oracle_outputs* out) {
+	int bins = s.bins;
+	s.bin_quads.assign(bins, {});
+	s.bin_tris.assign(bins, {});
+	// Small quads (bin_counter.glsl:64-80, bin_dispatcher.glsl:66-80): every bin of the AABB
+	for(int k = 0; k < s.nvis[0]; k++) {
+		uint32_t enc = s.quad_aabbs[k];
+		int x0, y0, x1, y1;
+		decodeAABB28(enc, x0, y0, x1, y1);
+		uint32_t entry = uint32_t(k) | (enc & 0xf0000000u);
+		for(int by = y0; by <= y1; by++)
+			for(int bx = x0; bx <= x1; bx++)
+				s.bin_quads[by * s.bcx + bx].push_back(entry);
+	}
+	// Large tris (bin_counter.glsl:112-134, bin_dispatcher.glsl:89-114): bin rows by scanline
+	for(int k = 0; k < s.nvis[1]; k++) {
+		int quad_idx = (s.mvq - 1) - k;
+		uint32_t enc = s.quad_aabbs[quad_idx];
+		for(int second = 0; second < 2; second++) {
+			if((enc >> (30 + second)) & 1u)
+				continue;
+			uint32_t tri_idx = uint32_t(quad_idx) * 2 + second;
+			int x0, y0, x1, y1;
+			decodeAABB28(enc, x0, y0, x1, y1);
+			int bsy, bey;
+			BinScan p = loadScanlineParamsBin(&s.tri_scan[size_t(tri_idx) * 8], bsy, bey);
+			for(int by = bsy; by <= bey; by++) {
+				int bmin, bmax;
+				scanlineStep(p, bmin, bmax);
+				bmin = std::max(bmin, x0), bmax = std::min(bmax, x1);
+				for(int bx = bmin; bx <= bmax; bx++)
+					s.bin_tris[by * s.bcx + bx].push_back(tri_idx);
+			}
+		}
+	}
+	// bin_categorizer.glsl:22-89: offsets (exclusive scan) and levels (LOW < threshold)
+	std::vector<uint32_t> cnt(size_t(bins) * 10, 0);
+	uint32_t qoff = 0, toff = 0;
+	int level_counts[5] = {0, 0, 0, 0, 0};
+	std::vector<uint32_t> low, high;
+	for(int b = 0; b < bins; b++) {
+		auto& q = s.bin_quads[b];
+		auto& t = s.bin_tris[b];
+		auto by_slot = [](uint32_t a, uint32_t b) { return (a & 0x0fffffffu) < (b & 0x0fffffffu); };
+		std::sort(q.begin(), q.end(), by_slot);
+		std::sort(t.begin(), t.end());
+		uint32_t nq = uint32_t(q.size()), nt = uint32_t(t.size());
+		cnt[bins * 0 + b] = nq;
+		cnt[bins * 1 + b] = qoff;
+		cnt[bins * 2 + b] = qoff + nq;
+		cnt[bins * 3 + b] = nt;
+		cnt[bins * 4 + b] = toff;
+		cnt[bins * 5 + b] = toff + nt;
+		qoff += nq, toff += nt;
+		int64_t num_tris = int64_t(nt) + int64_t(nq) * 2;
+		if(num_tris == 0)
+			level_counts[LUCID_BIN_LEVEL_EMPTY]++;
+		else if(num_tris < s.in->low_high_threshold)
+			low.push_back(uint32_t(b)), level_counts[LUCID_BIN_LEVEL_LOW]++;
+		else
+			high.push_back(uint32_t(b)), level_counts[LUCID_BIN_LEVEL_HIGH]++;
+	}
+	for(size_t i = 0; i < low.size(); i++)
+		cnt[size_t(bins) * 7 + i] = low[i];
+	for(size_t i = 0; i < high.size(); i++)
+		cnt[size_t(bins) * 9 + i] = high[i];
+	for(int i = 0; i < 5; i++)
+		out->bin_level_counts[i] = level_counts[i];
+	out->num_bin_quads = qoff;
+	out->num_bin_tris = toff;
+	out->bin_count = bins, out->bin_count_x = s.bcx, out->bin_count_y = s.bcy;
+	if(out->bin_counters)
+		memcpy(out->bin_counters, cnt.data(), cnt.size() * 4);
+	if(out->bin_quads && int64_t(qoff) <= out->bin_refs_capacity) {
+		size_t o = 0;
+		for(int b = 0; b < bins; b++)
+			for(uint32_t e : s.bin_quads[b])
+				out->bin_quads[o++] = e;
+	}
+	if(out->bin_tris && int64_t(toff) <= out->bin_refs_capacity) {
+		size_t o = 0;
+		for(int b = 0; b < bins; b++)
+			for(uint32_t e : s.bin_tris[b])
+				out->bin_tris[o++] = e;
+	}
+}
+
+// ---------------------------------------------------------------------------------------------
+// Raster (exact per-pixel order). Coverage follows raster_low.glsl:39-64 (generateRowTris):
+// the scan starts at the tri's first 8-row block row inside the bin and steps one row at a
+// time (rasterBinStep, raster.glsl:116-140). Depth and colour follow shading.glsl:107-165.
+
+struct RowSpan {
+	int lo, hi; // inclusive local x range, lo > hi means empty
+};
+
+// Per-row spans of one tri inside one bin; rows outside [row0, row1] are empty.
+void triBinRows(const uint32_t* sc, int bin_x, int bin_y, RowSpan rows[32]) {
+	for(int r = 0; r < 32; r++)
+		rows[r] = RowSpan{31, 0};
+	int ymin = int(sc[3] & 0xffffu) - bin_y, ymax = int(sc[3] >> 16) - bin_y;
+	int min_by = std::min(std::max(ymin, 0), 31) >> 3;
+	int max_by = std::min(std::max(ymax, 0), 31) >> 3;
+	float sx = float(bin_x), sy = float(bin_y + min_by * 8);
+	float mn[3], mx[3], step[3];
+	uint32_t sg = sc[7];
+	const float inf = INFINITY;
+	for(int i = 0; i < 3; i++) {
+		step[i] = bitsf(sc[4 + i]);
+		// loadScanlineParamsRow (scanline.glsl:13-26): scan += step * start.y - start.x
+		float scan = bitsf(sc[i]) + (step[i] * sy - sx);
+		bool xneg = (sg >> i) & 1u;
+		mn[i] = xneg ? -inf : scan;
+		mx[i] = xneg ? scan : inf;
+	}
+	for(int row = min_by * 8; row < max_by * 8 + 8; row++) {
+		float fl = fmaxf(fmaxf(mn[0], mn[1]), fmaxf(mn[2], 0.0f));
+		float fh = fminf(fminf(mx[0], mx[1]), fminf(mx[2], float(kBinSize)));
+		// Non-finite or out-of-range spans clamp to empty instead of wrapping.
+		int lo = f2i(fminf(fl, 33.0f));
+		int hi = f2i(fmaxf(fh, -1.0f)) - 1;
+		if(lo > hi)
+			lo = 31, hi = 0;
+		for(int i = 0; i < 3; i++)
+			mn[i] += step[i], mx[i] += step[i];
+		rows[row] = RowSpan{lo, hi};
+	}
+}
+
+struct Frag {
+	uint32_t key;   // nearFirstKey(inv_ray_pos)
+	uint32_t prim;  // input primitive id: input quad * 2 + second
+	uint32_t tri;   // tri slot
+	float depth;    // inv_ray_pos
+};
+
+void shadeFragment(const State& s, const Frag& f, int px, int py, float col[4]) {
+	const oracle_inputs* in = s.in;
+	const uint32_t* d = &s.tri_depth[size_t(f.tri) * 4];
+	const uint32_t* b = &s.tri_bary[size_t(f.tri) * 8];
+	float fx = float(px), fy = float(py);
+	float ray_pos = 1.0f / f.depth;
+	float e0 = bitsf(b[0]) * fx + (bitsf(b[1]) * fy + bitsf(b[2]));
+	float e1 = bitsf(b[4]) * fx + (bitsf(b[5]) * fy + bitsf(b[6]));
+	float b0 = e0 * ray_pos, b1 = e1 * ray_pos;
+	b0 = b0 - bitsf(b[3]);
+	b1 = b1 - bitsf(b[7]);
+	uint32_t flags = d[3] & 0xffffu, inst = d[3] >> 16;
+	col[0] = col[1] = col[2] = col[3] = 1.0f;
+	if((flags & LUCID_INST_HAS_COLOR) && in->instance_colors)
+		decodeRGBA8(in->instance_colors[inst], col);
+	if(flags & LUCID_INST_HAS_VERTEX_COLORS) {
+		uint32_t quad = f.tri >> 1, second = f.tri & 1;
+		float c[3][4];
+		uint32_t vid[3] = {s.quad_verts[size_t(quad) * 4 + 0],
+						   s.quad_verts[size_t(quad) * 4 + 1 + second],
+						   s.quad_verts[size_t(quad) * 4 + 2 + second]};
+		for(int k = 0; k < 3; k++) {
+			if(in->color_format == LUCID_COLOR_RGBA8) {
+				decodeRGBA8(((const uint32_t*)in->colors)[vid[k]], c[k]);
+			} else if(in->color_format == LUCID_COLOR_RGBA16F) {
+				const uint16_t* h = (const uint16_t*)in->colors + size_t(vid[k]) * 4;
+				for(int j = 0; j < 4; j++)
+					c[k][j] = halfToFloat(h[j]);
+			} else {
+				const float* fc = (const float*)in->colors + size_t(vid[k]) * 4;
+				for(int j = 0; j < 4; j++)
+					c[k][j] = fc[j];
+			}
+		}
+		float wgt = (1.0f - b0) - b1;
+		for(int j = 0; j < 4; j++)
+			col[j] = col[j] * (wgt * c[0][j] + (b0 * c[1][j] + b1 * c[2][j]));
+	}
+	if(in->tri_opacity)
+		col[3] = col[3] * in->tri_opacity[f.prim];
+}
+
+void rasterBin(const State& s, int bin, oracle_outputs* out, std::vector<std::vector<Frag>>& px,
+			   uint64_t& nfrag, uint64_t& nhbt, uint32_t& maxfrag) {
+	const oracle_inputs* in = s.in;
+	int bx = bin % s.bcx, by = bin / s.bcx;
+	int bin_x = bx * kBinSize, bin_y = by * kBinSize;
+	for(auto& v : px)
+		v.clear();
+	std::vector<uint32_t> tris;
+	for(uint32_t e : s.bin_quads[bin]) {
+		uint32_t quad = e & 0x0fffffffu;
+		for(int second = 0; second < 2; second++)
+			if(!((e >> (30 + second)) & 1u))
+				tris.push_back(quad * 2 + second);
+	}
+	for(uint32_t t : s.bin_tris[bin])
+		tris.push_back(t);
+	RowSpan rows[32];
+	for(uint32_t t : tris) {
+		const uint32_t* sc = &s.tri_scan[size_t(t) * 8];
+		triBinRows(sc, bin_x, bin_y, rows);
+		const uint32_t* d = &s.tri_depth[size_t(t) * 4];
+		float dx = bitsf(d[0]), dy = bitsf(d[1]), dz = bitsf(d[2]);
+		uint32_t prim = s.quad_source[t >> 1] * 2 + (t & 1);
+		for(int band = 0; band < 8; band++) {
+			uint32_t colmask = 0;
+			for(int r = band * 4; r < band * 4 + 4; r++) {
+				RowSpan sp = rows[r];
+				if(sp.lo > sp.hi)
+					continue;
+				colmask |= ((0xfu << (sp.lo >> 3)) & (0xfu >> (3 - (sp.hi >> 3))));
+				int py = bin_y + r;
+				if(py >= s.h)
+					continue;
+				for(int x = sp.lo; x <= sp.hi; x++) {
+					int pxx = bin_x + x;
+					if(pxx >= s.w)
+						continue;
+					// shading.glsl:116
+					float inv_ray_pos = dx * float(pxx) + (dy * float(py) + dz);
+					px[r * 32 + x].push_back(Frag{nearFirstKey(inv_ray_pos), prim, t, inv_ray_pos});
+				}
+			}
+			nhbt += __builtin_popcount(colmask);
+		}
+	}
+	const float* bg = in->config->background_color;
+	bool additive = (in->flags & LUCID_OPT_ADDITIVE_BLENDING) != 0;
+	bool alpha_threshold = (in->flags & LUCID_OPT_ALPHA_THRESHOLD) != 0;
+	for(int r = 0; r < 32; r++) {
+		int py = bin_y + r;
+		if(py >= s.h)
+			break;
+		for(int x = 0; x < 32; x++) {
+			int pxx = bin_x + x;
+			if(pxx >= s.w)
+				break;
+			auto& fr = px[r * 32 + x];
+			std::sort(fr.begin(), fr.end(), [](const Frag& a, const Frag& b) {
+				return a.key != b.key ? a.key < b.key : a.prim < b.prim;
+			});
+			nfrag += fr.size();
+			maxfrag = std::max(maxfrag, uint32_t(fr.size()));
+			size_t pix = size_t(py) * s.w + pxx;
+			if(out->frag_counts)
+				out->frag_counts[pix] = int32_t(fr.size());
+			if(out->frag_prims) {
+				int32_t* dst = out->frag_prims + pix * out->max_per_pixel;
+				for(int i = 0; i < out->max_per_pixel; i++)
+					dst[i] = i < int(fr.size()) ? int32_t(fr[i].prim) : -1;
+			}
+			// shading.glsl:279-280,312 in FP32 (and FP64 over the same FP32 colours)
+			float oc[3] = {0.0f, 0.0f, 0.0f}, T = 1.0f;
+			double oc64[3] = {0.0, 0.0, 0.0}, T64 = 1.0;
+			for(const Frag& f : fr) {
+				float c[4];
+				shadeFragment(s, f, pxx, py, c);
+				if(additive) {
+					for(int j = 0; j < 3; j++) {
+						oc[j] = oc[j] + c[j] * c[3];
+						oc64[j] = oc64[j] + double(c[j]) * double(c[3]);
+					}
+				} else {
+					for(int j = 0; j < 3; j++) {
+						oc[j] = oc[j] + (c[j] * c[3]) * T;
+						oc64[j] = oc64[j] + (double(c[j]) * double(c[3])) * T64;
+					}
+					T = T * (1.0f - c[3]);
+					T64 = T64 * (1.0 - double(c[3]));
+					if(alpha_threshold && T < (1.0f / 128.0f))
+						break;
+				}
+			}
+			float* img = out->image ? out->image + pix * 4 : nullptr;
+			double* img64 = out->image64 ? out->image64 + pix * 4 : nullptr;
+			for(int j = 0; j < 3; j++) {
+				float v = oc[j] + T * bg[j];
+				double v64 = oc64[j] + T64 * double(bg[j]);
+				if(img)
+					img[j] = fminf(fmaxf(v, 0.0f), 1.0f);
+				if(img64)
+					img64[j] = std::min(std::max(v64, 0.0), 1.0);
+			}
+			if(img)
+				img[3] = 1.0f;
+			if(img64)
+				img64[3] = 1.0;
+		}
+	}
+}
+
+void raster(State& s, oracle_outputs* out) {
+	const oracle_inputs* in = s.in;
+	std::vector<int> bins;
+	if(in->bin_subset) {
+		for(int i = 0; i < in->num_bin_subset; i++)
+			if(in->bin_subset[i] >= 0 && in->bin_subset[i] < s.bins)
+				bins.push_back(in->bin_subset[i]);
+	} else {
+		for(int b = 0; b < s.bins; b++)
+			bins.push_back(b);
+	}
+	int nt = std::max(1, in->num_threads);
+	std::atomic<size_t> next{0};
+	std::vector<uint64_t> nf(nt, 0), nh(nt, 0);
+	std::vector<uint32_t> mf(nt, 0);
+	auto worker = [&](int tid) {
+		std::vector<std::vector<Frag>> px(1024);
+		while(true) {
+			size_t i = next.fetch_add(1);
+			if(i >= bins.size())
+				break;
+			rasterBin(s, bins[i], out, px, nf[tid], nh[tid], mf[tid]);
+		}
+	};
+	if(nt == 1)
+		worker(0);
+	else {
+		std::vector<std::thread> th;
+		for(int t = 0; t < nt; t++)
+			th.emplace_back(worker, t);
+		for(auto& t : th)
+			t.join();
+	}
+	out->num_fragments = 0, out->num_hblock_tris = 0, out->max_pixel_fragments = 0;
+	for(int t = 0; t < nt; t++) {
+		out->num_fragments += nf[t];
+		out->num_hblock_tris += nh[t];
+		out->max_pixel_fragments = std::max(out->max_pixel_fragments, mf[t]);
+	}
+}
+
+} // namespace
+
+extern "C" int oracle_version(void) { return 1; }
+
+extern "C" int oracle_run(const oracle_inputs* in, oracle_outputs* out) {
+	if(!in || !out || !in->config || in->width <= 0 || in->height <= 0 ||
+	   in->max_visible_quads <= 0 || in->order_mode != 0)
+		return 1;
+	if(in->num_quads > 0 && (!in->positions || !in->quads_ib || !in->instances))
+		return 1;
+	State s;
+	s.in = in;
+	s.w = in->width, s.h = in->height;
+	s.bcx = (s.w + kBinSize - 1) / kBinSize;
+	s.bcy = (s.h + kBinSize - 1) / kBinSize;
+	s.bins = s.bcx * s.bcy;
+	s.mvq = in->max_visible_quads;
+	const lucid_frustum& fr = in->config->frustum;
+	s.origin = xyz(fr.ws_origin0);
+	s.dir0 = xyz(fr.ws_dir0);
+	s.dirx = xyz(fr.ws_dirx);
+	s.diry = xyz(fr.ws_diry);
+	// quad_setup.glsl:397-398: ray through the centre of pixel (0, 0)
+	V3 dxy = add(s.dirx, s.diry);
+	s.ray_dir0 = add(s.dir0, mul(dxy, 0.5f));
+	out->error_code = 0;
+	quadSetup(s, out);
+	binning(s, out);
+	auto copy = [](uint32_t* dst, const std::vector<uint32_t>& src) {
+		if(dst)
+			memcpy(dst, src.data(), src.size() * 4);
+	};
+	copy(out->quad_aabbs, s.quad_aabbs);
+	copy(out->quad_source, s.quad_source);
+	copy(out->quad_colors, s.quad_colors);
+	copy(out->quad_verts, s.quad_verts);
+	copy(out->tri_bary, s.tri_bary);
+	copy(out->tri_scan, s.tri_scan);
+	copy(out->tri_depth, s.tri_depth);
+	copy(out->tri_normals, s.tri_normals);
+	if(out->image || out->frag_counts || out->image64 || out->frag_prims)
+		raster(s, out);
+	return 0;
+}

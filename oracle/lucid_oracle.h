@@ -1,0 +1,99 @@
+/*
+ * Scalar CPU oracle of LucidRaster's compute rasterization path.
+ *
+ * TEST INFRASTRUCTURE ONLY: this library is the checker for the CUDA path and the timed CPU
+ * baseline. Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load it.
+ * Nothing in the lucid_gb300 package links, imports or calls it.
+ *
+ * Parity status: UNPINNED against the reference's own outputs. The reference runs only as
+ * Vulkan GLSL compute shaders on top of libfwk (absent), and has no tests or golden vectors,
+ * so this restatement is checked against hand-derived known-answer cases and invariants of
+ * the reference (src/lucid_renderer.cpp:629-707 offset checks) instead.
+ *
+ * Layout conventions shared with the CUDA path (both follow the reference):
+ *   - quad slot k < num_visible[0] holds the k-th visible small quad in input order;
+ *     slot MAX_VISIBLE_QUADS-1-k the k-th visible large quad (quad_setup.glsl:437-444),
+ *   - tri slot = quad slot * 2 + second_tri,
+ *   - records follow quad_setup.glsl:274-340 bit for bit.
+ */
+#ifndef LUCID_ORACLE_H
+#define LUCID_ORACLE_H
+
+#include <stdint.h>
+#include "../include/lucid_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct oracle_inputs {
+	int32_t width, height;
+	int32_t max_visible_quads;
+	int32_t low_high_threshold; /* 1024 in the reference */
+	uint32_t flags;             /* LUCID_OPT_* (additive blending, alpha threshold)          */
+	int32_t order_mode;         /* 0: exact per-pixel order, 1: reference 3-deep window      */
+	const float* positions;
+	const void* colors;
+	int32_t color_format;
+	int32_t num_verts;
+	const uint32_t* quads_ib;
+	int32_t num_quads;
+	int32_t num_instances;
+	const lucid_instance* instances;
+	const uint32_t* instance_colors;
+	const float* tri_opacity;
+	const lucid_config* config;
+	/* raster only these bins (ascending bin ids); NULL = all bins */
+	const int32_t* bin_subset;
+	int32_t num_bin_subset;
+	int32_t num_threads; /* raster worker threads (>= 1) */
+} oracle_inputs;
+
+typedef struct oracle_outputs {
+	/* ---- quad setup (sizes: MAX_VISIBLE_QUADS quads, 2*MAX_VISIBLE_QUADS tris) ---- */
+	int32_t num_input_quads;
+	int32_t num_visible[2];
+	uint32_t rejected[LUCID_REJECTION_TYPE_COUNT];
+	uint32_t error_code;
+	uint32_t num_binning_dispatches;
+	uint32_t* quad_aabbs;   /* [mvq]     may be NULL */
+	uint32_t* quad_source;  /* [mvq]                 */
+	uint32_t* quad_colors;  /* [mvq*4]               */
+	uint32_t* quad_verts;   /* [mvq*4]               */
+	uint32_t* tri_bary;     /* [2*mvq*8]             */
+	uint32_t* tri_scan;     /* [2*mvq*8]             */
+	uint32_t* tri_depth;    /* [2*mvq*4]             */
+	uint32_t* tri_normals;  /* [2*mvq]               */
+	/* ---- binning ---- */
+	int32_t bin_count, bin_count_x, bin_count_y;
+	uint32_t* bin_counters;    /* [10*bin_count] like g_counts (definitions.glsl:117-129)     */
+	uint32_t* bin_quads;       /* [bin quad refs], per bin sorted by slot                     */
+	uint32_t* bin_tris;        /* [bin tri refs], per bin sorted by slot                      */
+	int64_t bin_refs_capacity; /* capacity of bin_quads / bin_tris arrays                     */
+	int64_t num_bin_quads, num_bin_tris;
+	int32_t bin_level_counts[LUCID_BIN_LEVELS_COUNT];
+	/* ---- raster ---- */
+	float* image;          /* [h*w*4] may be NULL                                           */
+	double* image64;       /* [h*w*4] FP64 blend of the same ordered fragments, may be NULL */
+	int32_t* frag_counts;  /* [h*w] may be NULL                                              */
+	int32_t* frag_prims;   /* [h*w*max_per_pixel] may be NULL                                */
+	int32_t max_per_pixel;
+	uint64_t num_fragments;
+	uint64_t num_hblock_tris;
+	uint32_t max_pixel_fragments;
+	uint64_t invalid_pixels; /* reference-order mode: pixels whose window overflowed */
+} oracle_outputs;
+
+/* Runs setup, binning and (if out->image or out->frag_counts is set) the raster pass.
+ * Returns 0 on success, nonzero on invalid arguments. */
+int oracle_run(const oracle_inputs* in, oracle_outputs* out);
+
+/* Per-bin statistics of the binning result, used by scene reports: number of tris per bin
+ * (2*quads + tris) written into out[bin_count]. */
+int oracle_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,45 @@
+"""Shared helpers of the parity tests."""
+import os
+
+import numpy as np
+
+from lucid_gb300 import scenes
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def kat_cases():
+    data = np.load(os.path.join(GOLDEN, "kat.npz"))
+    names = sorted({k.split("/")[0] for k in data.files})
+    return {n: {k.split("/")[1]: data[k] for k in data.files if k.startswith(n + "/")} for n in names}
+
+
+def kat_scene(case):
+    w, h = (int(v) for v in case["size"])
+    return scenes.screen_triangles(case["tris"], case["colors"], w, h, tuple(case["bg"]))
+
+
+def canonical_quad_lists(counters, bin_count, lists):
+    """Per-bin sorted quad reference lists, keeping the cull-flag bits of every entry."""
+    cnt = counters[0:bin_count]
+    off = counters[bin_count:2 * bin_count]
+    res = []
+    for b in range(bin_count):
+        seg = np.asarray(lists[int(off[b]):int(off[b]) + int(cnt[b])], np.uint32)
+        order = np.argsort(seg & np.uint32(0x0FFFFFFF), kind="stable")
+        res.append(seg[order])
+    return res
+
+
+def canonical_tri_lists(counters, bin_count, lists):
+    cnt = counters[3 * bin_count:4 * bin_count]
+    off = counters[4 * bin_count:5 * bin_count]
+    return [np.sort(np.asarray(lists[int(off[b]):int(off[b]) + int(cnt[b])], np.uint32))
+            for b in range(bin_count)]
+
+
+def used_slots(nvis, mvq):
+    """Quad slot indices holding visible quads (small from 0 up, large from mvq-1 down)."""
+    small = np.arange(nvis[0])
+    large = mvq - 1 - np.arange(nvis[1])
+    return np.concatenate([small, large]).astype(np.int64)
