@@ -115,8 +115,9 @@ __device__ __forceinline__ uint32_t fbits(float f) { return __float_as_uint(f); 
 __device__ __forceinline__ float bitsf(uint32_t u) { return __uint_as_float(u); }
 
 // Ascending sort key that puts the nearest fragment (largest inv_ray_pos) first.
+// NaN depths (degenerate planes) use one canonical NaN so that CPU and GPU order them alike.
 __device__ __forceinline__ uint32_t nearFirstKey(float inv_ray_pos) {
-	uint32_t u = fbits(inv_ray_pos);
+	uint32_t u = inv_ray_pos != inv_ray_pos ? 0x7fc00000u : fbits(inv_ray_pos);
 	uint32_t asc = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
 	return ~asc;
 }

@@ -70,7 +70,7 @@ inline float bitsf(uint32_t u) {
 }
 // Ascending key of "nearest first": larger inv_ray_pos sorts first.
 inline uint32_t nearFirstKey(float inv_ray_pos) {
-	uint32_t u = fbits(inv_ray_pos);
+	uint32_t u = inv_ray_pos != inv_ray_pos ? 0x7fc00000u : fbits(inv_ray_pos);
 	uint32_t asc = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
 	return ~asc;
 }

@@ -38,6 +38,31 @@ def canonical_tri_lists(counters, bin_count, lists):
             for b in range(bin_count)]
 
 
+def assert_same_bits(got, want, msg=""):
+    """Bit-exact equality of u32 record arrays, except that two NaNs compare equal (the GPU's
+    canonical NaN is 0x7fffffff, x86's 0x7fc00000; both behave the same in every later use)."""
+    got = np.ascontiguousarray(got, np.uint32)
+    want = np.ascontiguousarray(want, np.uint32)
+    neq = got != want
+    if neq.any():
+        both_nan = np.isnan(got.view(np.float32)) & np.isnan(want.view(np.float32))
+        bad = neq & ~both_nan
+        if bad.any():
+            idx = np.argwhere(bad)[:5]
+            raise AssertionError(f"{msg}: {int(bad.sum())} mismatches, first at {idx.tolist()}: "
+                                 f"got {got[bad][:5]} want {want[bad][:5]}")
+
+
+def max_abs_diff(a, b):
+    """Max |a-b| where NaN == NaN (and NaN vs number counts as infinite)."""
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    both = np.isnan(a) & np.isnan(b)
+    d = np.abs(a - b)
+    d[both] = 0.0
+    d[np.isnan(d)] = np.inf
+    return float(d.max()) if d.size else 0.0
+
+
 def used_slots(nvis, mvq):
     """Quad slot indices holding visible quads (small from 0 up, large from mvq-1 down)."""
     small = np.arange(nvis[0])

@@ -66,7 +66,7 @@ def compare(scene, oracle, *, max_visible_quads=None, flags=0, dump=0, check_ima
     assert info.num_binning_dispatches[0] == o["num_binning_dispatches"]
     slots = helpers.used_slots(o["num_visible"], mvq)
     for key in ("quad_aabbs", "quad_source", "quad_verts"):
-        np.testing.assert_array_equal(g[key][slots], o[key][slots], err_msg=key)
+        helpers.assert_same_bits(g[key][slots], o[key][slots], key)
     if scene.color_format == scenes.COLOR_RGBA8:
         np.testing.assert_array_equal(g["quad_colors"][slots], o["quad_colors"][slots])
     tri_slots = []
@@ -77,7 +77,7 @@ def compare(scene, oracle, *, max_visible_quads=None, flags=0, dump=0, check_ima
                 tri_slots.append(2 * int(s) + second)
     tri_slots = np.array(tri_slots, np.int64)
     for key in ("tri_bary", "tri_scan", "tri_depth", "tri_normals"):
-        np.testing.assert_array_equal(g[key][tri_slots], o[key][tri_slots], err_msg=key)
+        helpers.assert_same_bits(g[key][tri_slots], o[key][tri_slots], key)
     # ---- binning
     n = o["bin_count"]
     gc, oc = g["bin_counters"], o["bin_counters"]
@@ -98,7 +98,7 @@ def compare(scene, oracle, *, max_visible_quads=None, flags=0, dump=0, check_ima
     assert info.num_hblock_tris == o["num_hblock_tris"]
     assert info.max_pixel_fragments == o["max_pixel_fragments"]
     if check_image:
-        err = np.abs(g["image"] - o["image"]).max() if g["image"].size else 0.0
+        err = helpers.max_abs_diff(g["image"], o["image"])
         assert err <= IMG_TOL, f"image max abs error {err}"
     if dump:
         np.testing.assert_array_equal(g["frag_counts"], o["frag_counts"])
