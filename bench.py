@@ -1,0 +1,363 @@
+"""Benchmark of the lucid_gb300 raster pipeline (one JSON line on rank 0).
+
+Workload: 1920x1080, 1M random triangles with heavy overdraw (Gaussian centres, sigma 0.2*W;
+log-normal area, median 60 px^2, sigma 2; 5% of triangles log-uniform in [10k, 50k] px^2;
+RGBA8, alpha U[0.1, 0.9]), exact per-pixel order, FP32 RGBA output. A step is one full frame
+(quad setup, bin count, categorize, dispatch, raster).
+
+value      fragments/s with the scene resident in device memory (CUDA events around each step
+           on the launching stream; L2 flushed by a 256 MB write between steps).
+e2e        same metric through lucid_render with host buffers: every step copies the scene from
+           pinned host memory and reads the FP32 image back.
+roofline   raster kernel (the dominant kernel): algorithmic bytes per launch / its measured time.
+cpu_baseline  the CPU oracle (port of the reference passes), all host threads, on a seeded
+           sample of bins; its frame time is extrapolated from the sample's fragments.
+
+--impl reference runs the CPU oracle only (the reference itself runs only as Vulkan GLSL).
+Multi-GPU (torchrun): independent replicas, one frame per rank per step ("scaling": "weak").
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "heavy1080"
+WORKLOAD_DESC = ("1920x1080, 1M random triangles: Gaussian centres (sigma 0.2*W), log-normal area "
+                 "(median 60 px^2, sigma 2) with 5% log-uniform in [10k,50k] px^2, view depth "
+                 "U[0.1,100], RGBA8 vertex colours, alpha U[0.1,0.9]; exact per-pixel order, FP32 RGBA")
+METRIC = "fragments_blended_per_s_1080p_1M_tris"
+UNIT = "fragments/s"
+KERNELS_PER_FRAME = 8  # setupPrep, setupClassify, setupScan, setupStore, binCount, binCategorize, binDispatch, raster
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="lucid_gb300", choices=["lucid_gb300", "reference"])
+    ap.add_argument("--cpu-sample-bins", type=int, default=0, help="bins in the CPU sample (0 = auto)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default=WORKLOAD,
+                    help="scenes.workload name (the default is the benchmark workload; smaller "
+                         "ones exist for profiler captures)")
+    return ap.parse_args()
+
+
+def workload_name(name):
+    return name + ": " + WORKLOAD_DESC if name == WORKLOAD else name
+
+
+def dist_setup(n_gpus):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic_per_fragment():
+    """DRAM bytes per fragment of the raster kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "raster_heavy1080.md")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        for line in f:
+            if line.startswith("traffic_bytes_per_fragment:"):
+                return float(line.split(":", 1)[1].split()[0])
+    return None
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for name, val in zip(names, parts[5:9]):
+                    if val.lower().startswith("active"):
+                        reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        load = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(load), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(scene, sample_bins, seed=0):
+    """Times the CPU oracle on all host threads: setup + binning on the whole scene, raster on a
+    seeded sample of bins; the raster time is extrapolated by the fraction of fragments."""
+    from oracle import binding
+    threads = os.cpu_count() or 1
+    mvq = max(1024, scene.num_quads)
+    t0 = time.perf_counter()
+    full = binding.run(scene, max_visible_quads=mvq, raster=False, setup_outputs=False)
+    t_bin = time.perf_counter() - t0
+    n = full["bin_count"]
+    c = full["bin_counters"]
+    rng = np.random.default_rng(seed)
+    k = min(n, sample_bins)
+    subset = np.sort(rng.choice(n, size=k, replace=False)).astype(np.int32)
+    t0 = time.perf_counter()
+    part = binding.run(scene, max_visible_quads=mvq, raster=True, bin_subset=subset,
+                       threads=threads, setup_outputs=False)
+    t_all = time.perf_counter() - t0
+    t_raster = max(t_all - t_bin, 1e-9)  # the sampled run repeats setup + binning
+    frag_sample = part["num_fragments"]
+    return dict(t_bin=t_bin, t_raster_sample=t_raster, frag_sample=frag_sample, bins=k,
+                bin_count=n, threads=threads,
+                tris_per_bin_sample=int((2 * c[:n][subset] + c[3 * n:4 * n][subset]).sum()))
+
+
+def run_reference(args, rank):
+    """--impl reference: the CPU oracle (port of the reference passes) on bounded samples."""
+    if rank != 0:
+        return
+    from lucid_gb300 import scenes
+    scene = scenes.workload(args.workload)
+    bins = args.cpu_sample_bins or 48
+    vals = []
+    last = None
+    for i in range(args.warmup + args.steps):
+        r = cpu_baseline(scene, bins, seed=i)
+        # extrapolated whole-frame rate: total fragments / (binning + raster of all bins)
+        rate = r["frag_sample"] / r["t_raster_sample"]
+        frame_frags = r["frag_sample"] * r["bin_count"] / r["bins"]
+        frame_time = r["t_bin"] + frame_frags / rate
+        if i >= args.warmup:
+            vals.append(frame_frags / frame_time)
+        last = r
+    value = float(np.mean(vals))
+    sample = (f"setup+binning of the full scene, raster of {last['bins']} seeded random bins "
+              f"of {last['bin_count']} per step; frame time extrapolated by fragments")
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": workload_name(args.workload)}, "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": last["threads"], "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    rank, world, local = dist_setup(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    from lucid_gb300 import build as lucid_build
+    if rank == 0:
+        lucid_build.build()
+    if dist is not None:
+        dist.barrier()
+    from lucid_gb300 import scenes, _lib
+    from lucid_gb300.renderer import FrameInputs, LucidRenderer
+
+    # replicas: each rank renders its own seeded frame of the same workload
+    scene = scenes.workload(args.workload, seed=1 + rank)
+    r = LucidRenderer(scene.width, scene.height, max_input_quads=scene.num_quads,
+                      max_visible_quads=scene.num_quads, max_bin_refs=8 * scene.num_quads)
+    frame = FrameInputs.from_scene(scene)
+    out = r.new_image()
+    stream = torch.cuda.current_stream()
+    flush_buf = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    # correctness of the frame and its counts
+    r.render(frame, out)
+    info, counters = r.info()
+    if info.error_code != 0:
+        raise RuntimeError(f"device error {_lib.ERR_NAMES.get(info.error_code)} {tuple(info.error_detail)}")
+    fragments = int(info.num_fragments)
+    hblock_tris = int(info.num_hblock_tris)
+    qrefs, trefs = int(info.num_bin_quad_refs), int(info.num_bin_tri_refs)
+    bq = r.download(_lib.BUF_BIN_QUADS, count=qrefs)
+    culled = int(np.count_nonzero((bq >> 30) & 1) + np.count_nonzero((bq >> 31) & 1))
+    bin_tris = 2 * qrefs - culled + trefs
+
+    for _ in range(args.warmup):
+        flush_buf.fill_(1)
+        r.render(frame, out)
+    torch.cuda.synchronize()
+
+    # ---- timed region: K frames, device-resident inputs
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        for i in range(args.steps):
+            flush_buf.fill_(i & 0xFF)
+            starts[i].record(stream)
+            r.render(frame, out)
+            ends[i].record(stream)
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = float(sum(step_ms))
+    if dist is not None:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = fragments * args.steps * world / (total_ms / 1e3)
+
+    # ---- raster kernel alone (roofline): pass-level API, events around lucid_raster
+    r.quad_setup(frame)
+    r.bin_count()
+    r.bin_categorize()
+    r.bin_dispatch()
+    ras_ms = []
+    for i in range(max(3, args.steps)):
+        flush_buf.fill_(i & 0xFF)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        r.raster(frame, out)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ras_ms.append(e0.elapsed_time(e1))
+    raster_ms = float(np.median(ras_ms))
+    w, h = scene.width, scene.height
+    alg_bytes = 4 * (qrefs + trefs) + 32 * bin_tris + 68 * hblock_tris + 16 * w * h
+    peak, peak_kind = measured_peaks()
+    achieved = alg_bytes / (raster_ms / 1e3) / 1e9
+    tpf = profile_traffic_per_fragment()
+    roofline = {"kernel": "rasterKernel", "bound": "hbm", "achieved": achieved, "peak": peak,
+                "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                "traffic": None if tpf is None else tpf * fragments,
+                "algorithmic_bytes": alg_bytes, "kernel_ms": raster_ms}
+
+    # ---- e2e: host buffers through lucid_render
+    host = {k: getattr(frame, k).cpu().pin_memory() for k in
+            ("positions", "colors", "quads", "instances", "instance_colors")}
+    host_out = torch.empty(out.shape, dtype=out.dtype).pin_memory()
+    h2d = sum(t.numel() * t.element_size() for t in host.values())
+    d2h = host_out.numel() * host_out.element_size()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for i in range(args.warmup + args.steps):
+        if i == args.warmup:
+            torch.cuda.synchronize()
+            e0.record(stream)
+        for k, t in host.items():
+            getattr(frame, k).copy_(t, non_blocking=True)
+        r.render(frame, out)
+        host_out.copy_(out, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    e2e_value = fragments * world / (e2e_ms / 1e3)
+
+    # ---- CPU baseline (rank 0, N=1 only)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        bins = args.cpu_sample_bins or 48
+        cb = cpu_baseline(scene, bins)
+        rate = cb["frag_sample"] / cb["t_raster_sample"]
+        frame_time = cb["t_bin"] + fragments / rate
+        cpu = {"value": fragments / frame_time, "unit": UNIT, "cores": cb["threads"], "kind": "port",
+               "sample": (f"oracle setup+binning of the whole frame ({cb['t_bin']:.2f} s) and raster "
+                          f"of {cb['bins']} seeded random bins of {cb['bin_count']} "
+                          f"({cb['frag_sample']} fragments, {cb['t_raster_sample']:.2f} s); frame "
+                          f"time extrapolated to {fragments} fragments"),
+               "ms_per_frame": frame_time * 1e3}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": workload_name(args.workload), "width": w, "height": h,
+                       "triangles": scene.num_tris, "fragments_per_frame": fragments,
+                       "max_fragments_per_pixel": int(info.max_pixel_fragments),
+                       "mean_layers_per_pixel": fragments / (w * h),
+                       "visible_quads": list(info.num_visible_quads),
+                       "bin_levels": {"low": info.bin_level_counts[2], "high": info.bin_level_counts[4]},
+                       "l2": "flushed between steps (256 MB write, outside the step events)",
+                       "parallelism": f"replicas x{world}"},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms},
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "clocks": clocks.summary(),
+            "gpu_launches": KERNELS_PER_FRAME * args.steps,
+            "mtri_per_s": scene.num_tris * args.steps * world / (total_ms / 1e3) / 1e6,
+        }
+        print(json.dumps(line), flush=True)
+    r.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -105,7 +105,7 @@ class LucidRenderer:
         self.width, self.height = int(width), int(height)
         self.bin_count_x = (self.width + 31) // 32
         self.bin_count_y = (self.height + 31) // 32
-        self.bin_count = self.bin_count_x * self.bin_count_y
+        self.num_bins = self.bin_count_x * self.bin_count_y
         torch.cuda.current_device()  # make sure the primary context exists
         h = ctypes.c_void_p()
         check(self.lib.lucid_create(ctypes.byref(o), self.width, self.height, ctypes.byref(h)),
@@ -176,7 +176,7 @@ class LucidRenderer:
     # -- info / statistics ------------------------------------------------------------------
     def info(self, stream=None):
         info = _lib.Info()
-        counters = np.zeros(10 * self.bin_count, np.uint32)
+        counters = np.zeros(10 * self.num_bins, np.uint32)
         check(self.lib.lucid_get_info(self.handle, ctypes.byref(info), counters.ctypes.data,
                                       _stream_ptr(stream)), "lucid_get_info")
         return info, counters
@@ -195,7 +195,7 @@ class LucidRenderer:
         """Offset consistency checks of LucidRenderer::verifyInfo (src/lucid_renderer.cpp:629-707).
         Returns a list of error strings (empty when consistent)."""
         _, c = self.info(stream)
-        n = self.bin_count
+        n = self.num_bins
         errors = []
         for base, name in ((0, "quad"), (3, "tri")):
             cnt = c[n * base:n * (base + 1)].astype(np.int64)
@@ -210,7 +210,7 @@ class LucidRenderer:
     def stats(self, stream=None):
         """Counters reported by LucidRenderer::getStats (src/lucid_renderer.cpp:709-836)."""
         info, c = self.info(stream)
-        n = self.bin_count
+        n = self.num_bins
         quad_counts, tri_counts = c[:n], c[3 * n:4 * n]
         npix = self.width * self.height
         return dict(

@@ -392,6 +392,10 @@ def workload(name: str, seed: int | None = None) -> Scene:
         return random_tris(1920, 1080, 1_000_000, seed=1 if seed is None else seed,
                            center_sigma=0.2 * 1920, area_median=60.0, area_sigma=2.0,
                            alpha_range=(0.1, 0.9), large_fraction=0.05)
+    if name == "heavy1080_small":  # same distributions, 250k triangles (profiling captures)
+        return random_tris(1920, 1080, 250_000, seed=1 if seed is None else seed,
+                           center_sigma=0.2 * 1920, area_median=60.0, area_sigma=2.0,
+                           alpha_range=(0.1, 0.9), large_fraction=0.05)
     if name == "meshes4k":
         return meshes(seed=2 if seed is None else seed)
     if name == "grad512":
