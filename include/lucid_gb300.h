@@ -359,6 +359,34 @@ lucid_status lucid_autotune(lucid_renderer* renderer, const lucid_frame_inputs* 
 							float* scratch_rgba, int32_t* out_ctas_per_sm,
 							int32_t* out_low_high_threshold, void* stream);
 
+/* ---------------------------------------------------------------------------------------- */
+/* Binning without allocation. No counterpart in the reference.
+ *
+ * For callers that cannot call cudaMalloc: a host whose allocator owns all device memory, or
+ * code that records GPU work while allocating is not allowed. Runs the bin counter,
+ * categorizer and dispatcher on caller-provided device buffers; their remaining scratch (the
+ * counter's per-CTA bin histograms, the status block, the bin work list) is a static device
+ * array of 1 MiB held by every GPU that loads the library.
+ *
+ * Inputs (device): quad_aabbs (max_visible_quads u32, layout of LUCID_BUF_QUAD_AABBS) and
+ * tri_scan (2*max_visible_quads records of 8 u32, LUCID_BUF_TRI_SCAN, 16-byte aligned) of a
+ * quad setup with num_small_quads / num_large_quads visible quads.
+ * Outputs (device): bin_counters (10 * bin count u32, the g_counts layout), bin_quads and
+ * bin_tris (max_bin_refs u32 each), optional info_out (one lucid_info: level counts, error
+ * code).
+ * Limit: at most LUCID_NOALLOC_MAX_BINS 32x32 bins (e.g. 1920x1080 = 2040 bins); larger
+ * viewports return LUCID_CAPACITY_EXCEEDED. All calls share the static scratch: calls whose
+ * work overlaps on the GPU race; calls on one stream are ordered. The first call on each
+ * device looks the scratch up with cudaGetSymbolAddress, so make it before any stream capture.
+ * Calls no cudaMalloc or cudaFree. */
+#define LUCID_NOALLOC_MAX_BINS 2048
+lucid_status lucid_bin_noalloc(const uint32_t* quad_aabbs, const uint32_t* tri_scan,
+							   int32_t num_small_quads, int32_t num_large_quads,
+							   int32_t max_visible_quads, int32_t width, int32_t height,
+							   int32_t low_high_threshold, uint32_t* bin_counters,
+							   uint32_t* bin_quads, uint32_t* bin_tris, int32_t max_bin_refs,
+							   lucid_info* info_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -110,6 +110,9 @@ SIGNATURES = [
     ("lucid_render_batch", c_int32, [c_void_p, ctypes.POINTER(ViewC), c_int32, c_void_p]),
     ("lucid_autotune", c_int32, [c_void_p, ctypes.POINTER(FrameInputsC), c_void_p,
                                  ctypes.POINTER(c_int32), ctypes.POINTER(c_int32), c_void_p]),
+    ("lucid_bin_noalloc", c_int32, [c_void_p, c_void_p, c_int32, c_int32, c_int32, c_int32,
+                                    c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_int32,
+                                    c_void_p, c_void_p]),
 ]
 
 _lib = None

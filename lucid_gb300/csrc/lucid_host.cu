@@ -58,6 +58,8 @@ template <typename T> size_t bytesOf(size_t n) { return n * sizeof(T); }
 
 } // namespace
 
+void lucidSetLastError(const std::string& msg) { g_last_error = msg; }
+
 struct lucid_renderer {
 	lucid_options opts;
 	int width, height;
