@@ -181,7 +181,10 @@ typedef struct lucid_info {
 	uint64_t num_hblock_tris; /* 64-bit stats[1]                                          */
 	uint32_t num_band_entries;
 	uint32_t num_views;
-	uint32_t ext_reserved[50];
+	uint64_t raster_windows;          /* depth windows processed by the raster pass         */
+	uint64_t raster_window_fragments; /* fragments sorted in those windows                  */
+	uint32_t raster_radix_windows;    /* windows sorted by the block-wide radix fallback    */
+	uint32_t ext_reserved[45];
 } lucid_info;
 
 #define LUCID_INFO_REFERENCE_WORDS 1152

@@ -60,7 +60,9 @@ class Info(ctypes.Structure):
         ("raster_work_counter", c_uint32), ("num_bin_quad_refs", c_uint32),
         ("num_bin_tri_refs", c_uint32), ("max_pixel_fragments", c_uint32),
         ("num_fragments", c_uint64), ("num_hblock_tris", c_uint64),
-        ("num_band_entries", c_uint32), ("num_views", c_uint32), ("ext_reserved", c_uint32 * 50)]
+        ("num_band_entries", c_uint32), ("num_views", c_uint32),
+        ("raster_windows", c_uint64), ("raster_window_fragments", c_uint64),
+        ("raster_radix_windows", c_uint32), ("ext_reserved", c_uint32 * 45)]
 
 
 assert ctypes.sizeof(Info) == 1216 * 4

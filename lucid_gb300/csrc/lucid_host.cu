@@ -201,6 +201,8 @@ lucid_status resetRasterCounters(lucid_renderer* r, cudaStream_t st) {
 	LUCID_CUDA_TRY(cudaMemsetAsync(&info->stats[0], 0, 8, st));
 	LUCID_CUDA_TRY(cudaMemsetAsync(&info->max_pixel_fragments, 0, 4, st));
 	LUCID_CUDA_TRY(cudaMemsetAsync(&info->num_fragments, 0, 16, st));
+	LUCID_CUDA_TRY(cudaMemsetAsync(info->raster_timers, 0, sizeof(info->raster_timers), st));
+	LUCID_CUDA_TRY(cudaMemsetAsync(&info->raster_windows, 0, 20, st));
 	return LUCID_OK;
 }
 

@@ -11,14 +11,22 @@
 //     layout of raster_high.glsl:85-88) in this CTA's band scratch; spans are clipped to the
 //     viewport. A shared +1/-1 difference array per row counts fragments per pixel.
 //  B. Pixel groups. The bin's pixels (row-major) are cut into groups of at most 256 pixels
-//     and kGroupCap fragments using the per-pixel prefix sum.
-//  C. Per group: fragments (32-bit nearest-first depth key, 32-bit payload = pixel | entry)
-//     are generated in shared memory, then sorted by a stable LSD radix sort on the depth key
-//     followed by the pixel index (5 passes of 8 bits, warp-match ranking); runs of equal
-//     depth are put in primitive-id order. Shading runs in parallel batches of 16 fragments
-//     per pixel; one thread per pixel blends front to back in FP32
-//     (out += rgb*a*T; T *= 1-a, shading.glsl:279-280) and stops once T == 0, after which no
-//     later fragment can change the result. Background is added last (shading.glsl:312).
+//     whose fragments, each pixel counted up to kWindow, fit kGroupBudget.
+//  C. Depth windows. A group whose pixels all have <= kWindow fragments is one window. In a
+//     heavier group every pixel gets a coarse histogram of its depth keys (buckets of the
+//     group's key range); a pixel's window is the run of buckets, from the first one it has
+//     not processed, that holds >= kWindow fragments. Buckets split the key space in order,
+//     so windows visit each pixel's fragments strictly front to back.
+//  D. Per window: fragments (32-bit nearest-first depth key, 32-bit payload = pixel | band |
+//     entry) are generated by one warp per pixel row (lane = pixel, band entries broadcast by
+//     shuffle) and written to their pixel's segment, in a heavy group to the sub-segment of
+//     their depth bucket. Sub-segments are sorted by key (one thread per small sub-segment with
+//     a register network, one warp per larger one with a bitonic network; a block-wide radix
+//     sort when one exceeds 256). Runs of equal depth are put in primitive-id order. Shading
+//     runs in parallel batches; one thread per pixel blends front to back in FP32
+//     (out += rgb*a*T; T *= 1-a, shading.glsl:279-280) and stops once T == 0: no later
+//     fragment can change the pixel (it adds rgb*a*0). Background is added last
+//     (shading.glsl:312).
 
 #include "lucid_common.cuh"
 #include "lucid_kernels.h"
@@ -27,29 +35,51 @@ namespace lucid {
 
 constexpr int RT = kRasterThreads;
 constexpr int NW = RT / 32;
-constexpr int kGroupCap = 8192;     // fragments per pixel group (shared-memory sort capacity)
+constexpr int kGroupCap = 8192;     // fragments per window (shared-memory sort capacity)
 constexpr int kGroupPixels = 256;   // pixels per group (8-bit pixel index in the payload)
-constexpr int kShadeBatch = 16;     // fragments per pixel per shading round
+constexpr int kStage = 4096;        // shaded fragments per shading round (64 KB of float4)
+constexpr int kWindow = 176;        // target fragments per pixel per depth window
+constexpr int kGroupBudget = 6144;  // sum over a group's pixels of min(count, kWindow)
+constexpr int kHistWords = 8192;    // per-group depth histogram (pixels x buckets)
 
 struct RasterSmem {
 	// kv[b][0] = keys, kv[b][1] = payloads of buffer b; the buffer not holding the sorted
-	// fragments doubles as the 64 KB shading stage (kGroupPixels * kShadeBatch float4).
+	// fragments doubles as the 64 KB shading stage.
 	uint32_t kv[2][2][kGroupCap];
+	// per-(pixel, bucket) fragment counts; inside a window the counts of its buckets become
+	// the sub-segment cursors
+	uint32_t hist[kHistWords];
 	uint32_t radix[256 * NW];
-	int pix_prefix[1025];
+	int pix_count[1024];
+	int eff_prefix[1025];
 	int row_diff[32 * 33];
 	float px_T[kGroupPixels];
 	float px_c[kGroupPixels][3];
-	int px_cursor[kGroupPixels];
+	int px_lo[kGroupPixels];     // first bucket not yet processed
+	int px_cut[kGroupPixels];    // last bucket of the current window (-1: not in the window)
+	int px_wbase[kGroupPixels];  // window segment start in the sort buffer
+	int px_wend[kGroupPixels];   // window segment end (generation cursor of light groups)
+	int px_wcnt[kGroupPixels];   // fragments of the pixel in the current window
+	int px_bcur[kGroupPixels];   // blend cursor
+	int px_done[kGroupPixels];   // fragments already processed (verification dump index)
+	int px_state[kGroupPixels];  // 0 active, 1 finished
+	// sub-segments of the current window that need sorting, as (start << 16 | count):
+	// counts 2..16 are sorted by one thread, 17..256 by one warp
+	uint32_t sub_small[kGroupCap / 2];
+	uint32_t sub_large[kGroupCap / 17 + 1];
+	int n_small, n_large;
 	int band_count[8];
 	int scan_tmp[NW + 1];
 	uint32_t scan_tmpu[NW + 1];
 	unsigned long long stat_hbt;
+	uint32_t kmin, kmax;
 	int bin;
 	int group_end;
-	int flag;
 	int single_digit;
+	int any_big;
 };
+
+static_assert(sizeof(RasterSmem) <= 227 * 1024, "raster shared memory exceeds one SM");
 
 size_t rasterSmemBytes() { return sizeof(RasterSmem); }
 int rasterThreads() { return RT; }
@@ -116,6 +146,19 @@ __device__ __forceinline__ uint32_t fragPrim(const FrameParams& p, const uint2* 
 	return __ldg(p.quad_source + (tri >> 1)) * 2 + (tri & 1);
 }
 
+// Lanes of the warp (within `act`) whose 8-bit digit equals this lane's: 8 ballots, one per bit.
+// Every lane of the warp must call it.
+__device__ __forceinline__ uint32_t digitPeers(uint32_t d, uint32_t act) {
+	uint32_t peers = act;
+#pragma unroll
+	for(int b = 0; b < 8; b++) {
+		bool bit = (d >> b) & 1u;
+		uint32_t m = __ballot_sync(0xffffffffu, bit);
+		peers &= bit ? m : ~m;
+	}
+	return peers;
+}
+
 // One stable LSD pass on 8-bit digits. Returns false (and leaves the data in place) when all
 // elements share the digit.
 __device__ bool radixPass(RasterSmem& s, int src, int n, int shift, bool pixel_digit) {
@@ -138,11 +181,9 @@ __device__ bool radixPass(RasterSmem& s, int src, int n, int shift, bool pixel_d
 		if(valid)
 			d = pixel_digit ? (vin[i] & 0xffu) : ((kin[i] >> shift) & 0xffu);
 		uint32_t act = __ballot_sync(0xffffffffu, valid);
-		if(valid) {
-			uint32_t peers = __match_any_sync(act, d);
-			if(lane == __ffs(peers) - 1)
-				s.radix[d * NW + warp] += __popc(peers);
-		}
+		uint32_t peers = digitPeers(d, act);
+		if(valid && lane == __ffs(peers) - 1)
+			s.radix[d * NW + warp] += __popc(peers);
 	}
 	__syncthreads();
 	// exclusive scan of radix[] in (digit, warp) order; 8 counters per thread
@@ -182,16 +223,16 @@ __device__ bool radixPass(RasterSmem& s, int src, int n, int shift, bool pixel_d
 			d = pixel_digit ? (v & 0xffu) : ((k >> shift) & 0xffu);
 		}
 		uint32_t act = __ballot_sync(0xffffffffu, valid);
-		if(valid) {
-			uint32_t peers = __match_any_sync(act, d);
-			uint32_t pos = s.radix[d * NW + warp] + __popc(peers & laneMaskLt());
-			__syncwarp(act);
-			if(lane == __ffs(peers) - 1)
-				s.radix[d * NW + warp] += __popc(peers);
-			if(pos < uint32_t(n)) {
-				kout[pos] = k;
-				vout[pos] = v;
-			}
+		uint32_t peers = digitPeers(d, act);
+		uint32_t pos = 0;
+		if(valid)
+			pos = s.radix[d * NW + warp] + __popc(peers & laneMaskLt());
+		__syncwarp();
+		if(valid && lane == __ffs(peers) - 1)
+			s.radix[d * NW + warp] += __popc(peers);
+		if(valid && pos < uint32_t(n)) {
+			kout[pos] = k;
+			vout[pos] = v;
 		}
 		__syncwarp();
 	}
@@ -199,9 +240,147 @@ __device__ bool radixPass(RasterSmem& s, int src, int n, int shift, bool pixel_d
 	return true;
 }
 
+// Sorts (key, payload) pairs [base, base+n) of shared memory ascending by key with one warp:
+// a bitonic network over 32*E registers (element i = e*32 + lane), padded with key 0xffffffff
+// (never produced by nearFirstKey). Equal keys keep no particular order. Called by all lanes.
+template <int E>
+__device__ __forceinline__ void warpSortSegment(uint32_t* K, uint32_t* V, int base, int n) {
+	const int lane = threadIdx.x & 31;
+	uint32_t k[E], v[E];
+#pragma unroll
+	for(int e = 0; e < E; e++) {
+		int i = e * 32 + lane;
+		k[e] = i < n ? K[base + i] : 0xffffffffu;
+		v[e] = i < n ? V[base + i] : 0u;
+	}
+#pragma unroll
+	for(int kk = 2; kk <= 32 * E; kk <<= 1) {
+#pragma unroll
+		for(int j = kk >> 1; j > 0; j >>= 1) {
+			if(j >= 32) {
+#pragma unroll
+				for(int e = 0; e < E; e++) {
+					int e2 = e ^ (j >> 5);
+					if(e2 > e) {
+						bool up = ((e * 32 + lane) & kk) == 0;
+						bool sw = up ? (k[e] > k[e2]) : (k[e] < k[e2]);
+						uint32_t tk = sw ? k[e2] : k[e], tv = sw ? v[e2] : v[e];
+						k[e2] = sw ? k[e] : k[e2], v[e2] = sw ? v[e] : v[e2];
+						k[e] = tk, v[e] = tv;
+					}
+				}
+			} else {
+				const bool lower = (lane & j) == 0;
+#pragma unroll
+				for(int e = 0; e < E; e++) {
+					uint32_t ok = __shfl_xor_sync(0xffffffffu, k[e], j);
+					uint32_t ov = __shfl_xor_sync(0xffffffffu, v[e], j);
+					bool up = ((e * 32 + lane) & kk) == 0;
+					bool take = lower == up ? ok < k[e] : ok > k[e];
+					k[e] = take ? ok : k[e];
+					v[e] = take ? ov : v[e];
+				}
+			}
+		}
+	}
+#pragma unroll
+	for(int e = 0; e < E; e++) {
+		int i = e * 32 + lane;
+		if(i < n) {
+			K[base + i] = k[e];
+			V[base + i] = v[e];
+		}
+	}
+}
+
+// Sorts a small segment [base, base+n), n <= N, by one thread: bitonic network in registers.
+template <int N>
+__device__ __forceinline__ void threadSortSegment(uint32_t* K, uint32_t* V, int base, int n) {
+	uint32_t k[N], v[N];
+#pragma unroll
+	for(int i = 0; i < N; i++) {
+		k[i] = i < n ? K[base + i] : 0xffffffffu;
+		v[i] = i < n ? V[base + i] : 0u;
+	}
+#pragma unroll
+	for(int kk = 2; kk <= N; kk <<= 1) {
+#pragma unroll
+		for(int j = kk >> 1; j > 0; j >>= 1) {
+#pragma unroll
+			for(int i = 0; i < N; i++) {
+				int l = i ^ j;
+				if(l > i) {
+					bool up = (i & kk) == 0;
+					bool sw = up ? (k[i] > k[l]) : (k[i] < k[l]);
+					uint32_t tk = sw ? k[l] : k[i], tv = sw ? v[l] : v[i];
+					k[l] = sw ? k[i] : k[l], v[l] = sw ? v[i] : v[l];
+					k[i] = tk, v[i] = tv;
+				}
+			}
+		}
+	}
+#pragma unroll
+	for(int i = 0; i < N; i++)
+		if(i < n) {
+			K[base + i] = k[i];
+			V[base + i] = v[i];
+		}
+}
+
 __device__ void writePixel(const FrameParams& p, int px, int py, float4 c) {
 	if(px < p.width && py < p.height)
 		reinterpret_cast<float4*>(p.out_rgba)[size_t(py) * p.width + px] = c;
+}
+
+// Visits every fragment of pixels [p0, p1) of the bin: fn(t, key, band, slot) with t the pixel
+// index inside the group, called by the lane owning pixel t. Warps are assigned to the group's
+// rows (lane = pixel column) and split a row's band entries; entries are loaded 32 at a time
+// (one per lane) and broadcast by shuffle. The key is evaluated exactly as in the oracle
+// (shading.glsl:116): dx * px + (dy * py + dz).
+template <typename Fn>
+__device__ __forceinline__ void forEachGroupFragment(const FrameParams& p, const RasterSmem& s,
+													  const uint2* scratch, int band_cap, int bin_x,
+													  int bin_y, int p0, int p1, Fn fn) {
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	const int r0 = p0 >> 5, r1 = (p1 - 1) >> 5;
+	const int nrows = r1 - r0 + 1;
+	const int per_row = NW / nrows; // >= 1: a group spans at most 9 rows
+	if(warp >= per_row * nrows)
+		return;
+	const int row = r0 + warp / per_row, slice = warp % per_row;
+	const int b = row >> 2, rshift = 5 * (row & 3);
+	const int ne = s.band_count[b];
+	const int jbeg = int((int64_t(ne) * slice) / per_row), jend = int((int64_t(ne) * (slice + 1)) / per_row);
+	const int pix = row * 32 + lane;
+	const bool in_group = pix >= p0 && pix < p1;
+	const int t = pix - p0;
+	const float fx = float(bin_x + lane), fy = float(bin_y + row);
+	for(int j0 = jbeg; j0 < jend; j0 += 32) {
+		const int j = j0 + lane;
+		uint2 e = make_uint2(0x1fu << 5 * 3, 0u); // empty spans for lanes past the end
+		float dx = 0.0f, dy = 0.0f, dz = 0.0f;
+		if(j < jend) {
+			e = scratch[size_t(b) * band_cap + j];
+			uint4 d = __ldg(p.tri_depth + entryTri(e));
+			dx = bitsf(d.x), dy = bitsf(d.y), dz = bitsf(d.z);
+		}
+		const int cnt = min(32, jend - j0);
+		for(int k = 0; k < cnt; k++) {
+			uint32_t ex = __shfl_sync(0xffffffffu, e.x, k), ey = __shfl_sync(0xffffffffu, e.y, k);
+			int lo = (ex >> rshift) & 31, hi = (ey >> rshift) & 31;
+			bool covered = in_group && lane >= lo && lane <= hi;
+			if(!__any_sync(0xffffffffu, covered))
+				continue;
+			float kdx = __shfl_sync(0xffffffffu, dx, k);
+			float kdy = __shfl_sync(0xffffffffu, dy, k);
+			float kdz = __shfl_sync(0xffffffffu, dz, k);
+			if(covered) {
+				float ty = kdy * fy + kdz;
+				float inv_ray_pos = kdx * fx + ty;
+				fn(t, nearFirstKey(inv_ray_pos), b, j0 + k);
+			}
+		}
+	}
 }
 
 __global__ void __launch_bounds__(RT, 1) rasterKernel(FrameParams p) {
@@ -215,12 +394,25 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(FrameParams p) {
 	const bool additive = (p.flags & LUCID_OPT_ADDITIVE_BLENDING) != 0;
 	const bool alpha_threshold = (p.flags & LUCID_OPT_ALPHA_THRESHOLD) != 0;
 	const bool dump = p.dump_counts != nullptr;
+	// Section timers (timers.glsl:9-39): thread 0 accumulates clock64 deltas between the
+	// CTA-wide barriers that separate the phases; units of 256 cycles in lucid_info.raster_timers:
+	// 0 row spans, 1 counts, 2 depth histograms, 3 window fragments, 4 sort, 5 shading,
+	// 6 blending, 7 output and bin fetch.
+	const bool timers = (p.flags & LUCID_OPT_TIMERS) != 0;
+	long long tacc[8] = {0, 0, 0, 0, 0, 0, 0, 0}, tlast = timers ? clock64() : 0;
+#define RASTER_TIMER(i)                                                                            \
+	do {                                                                                           \
+		if(timers && tid == 0) {                                                                   \
+			long long now__ = clock64();                                                           \
+			tacc[i] += now__ - tlast;                                                              \
+			tlast = now__;                                                                         \
+		}                                                                                          \
+	} while(0)
 
 	while(true) {
 		if(tid == 0) {
 			uint32_t w = atomicAdd(&p.info->raster_work_counter, 1u);
 			s.bin = w < uint32_t(p.bin_count) ? int(p.raster_work[w]) : -1;
-			s.flag = 0;
 			s.stat_hbt = 0;
 		}
 		if(tid < 8)
@@ -228,6 +420,7 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(FrameParams p) {
 		for(int i = tid; i < 32 * 33; i += RT)
 			s.row_diff[i] = 0;
 		__syncthreads();
+		RASTER_TIMER(7);
 		const int bin = s.bin;
 		if(bin < 0)
 			break;
@@ -305,42 +498,42 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(FrameParams p) {
 				}
 			}
 		}
-		// reduce half-block-tri counts
 #pragma unroll
 		for(int o = 16; o > 0; o >>= 1)
 			hbt += __shfl_xor_sync(0xffffffffu, hbt, o);
 		if(lane == 0 && hbt)
 			atomicAdd(&s.stat_hbt, hbt);
 		__syncthreads();
+		RASTER_TIMER(0);
 		bool overflow = !lists_ok;
 		for(int b = 0; b < 8; b++)
 			overflow |= s.band_count[b] > band_cap;
 		if(overflow) {
-			if(tid == 0) {
-				if(lists_ok)
-					raiseError(p.info, LUCID_ERR_BAND_ENTRIES, uint32_t(bin), 0, uint32_t(band_cap));
-			}
+			if(tid == 0 && lists_ok)
+				raiseError(p.info, LUCID_ERR_BAND_ENTRIES, uint32_t(bin), 0, uint32_t(band_cap));
 			for(int i = tid; i < 1024; i += RT)
 				writePixel(p, bin_x + (i & 31), bin_y + (i >> 5), make_float4(1.0f, 0.0f, 0.0f, 1.0f));
 			__syncthreads();
 			continue;
 		}
 
-		// ---- B. per-pixel counts and their prefix over the bin (row-major)
+		// ---- B. per-pixel counts; prefix of min(count, kWindow) for the groups
 		for(int row = warp; row < 32; row += NW) {
 			int v = s.row_diff[row * 33 + lane];
-			s.row_diff[row * 33 + lane] = warpInclusiveScan(v);
+			s.pix_count[row * 32 + lane] = warpInclusiveScan(v);
 		}
 		__syncthreads();
 		{
-			int c0 = s.row_diff[(2 * tid >> 5) * 33 + (2 * tid & 31)];
-			int c1 = s.row_diff[((2 * tid + 1) >> 5) * 33 + ((2 * tid + 1) & 31)];
+			int c0 = s.pix_count[2 * tid], c1 = s.pix_count[2 * tid + 1];
+			int e0 = min(c0, kWindow), e1 = min(c1, kWindow);
 			int total;
-			int off = blockExclusiveScan(c0 + c1, s.scan_tmp, &total);
-			s.pix_prefix[2 * tid] = off;
-			s.pix_prefix[2 * tid + 1] = off + c0;
+			int off = blockExclusiveScan(e0 + e1, s.scan_tmp, &total);
+			s.eff_prefix[2 * tid] = off;
+			s.eff_prefix[2 * tid + 1] = off + e0;
 			if(tid == 0)
-				s.pix_prefix[1024] = total;
+				s.eff_prefix[1024] = total;
+			int frags;
+			blockExclusiveScan(c0 + c1, s.scan_tmp, &frags);
 			int mx = max(c0, c1);
 #pragma unroll
 			for(int o = 16; o > 0; o >>= 1)
@@ -349,206 +542,384 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(FrameParams p) {
 				atomicMax(&p.info->max_pixel_fragments, uint32_t(mx));
 			if(tid == 0) {
 				unsigned long long hb = s.stat_hbt;
-				atomicAdd((unsigned long long*)&p.info->num_fragments, (unsigned long long)total);
+				atomicAdd((unsigned long long*)&p.info->num_fragments, (unsigned long long)frags);
 				atomicAdd((unsigned long long*)&p.info->num_hblock_tris, hb);
-				atomicAdd(&p.info->stats[0], uint32_t(total));
+				atomicAdd(&p.info->stats[0], uint32_t(frags));
 				atomicAdd(&p.info->stats[1], uint32_t(hb));
 			}
 		}
 		__syncthreads();
+		RASTER_TIMER(1);
 
 		// ---- C. pixel groups
 		int p0 = 0;
 		while(p0 < 1024) {
 			if(tid == 0) {
-				int base = s.pix_prefix[p0];
-				int limit = min(p0 + kGroupPixels, 1024);
-				int p1;
-				if(s.pix_prefix[p0 + 1] - base > kGroupCap) {
-					p1 = -(p0 + 1); // single pixel beyond capacity
-				} else {
-					int lo = p0 + 1, hi = limit; // largest p1 in [lo, hi] with count <= cap
-					while(lo < hi) {
-						int mid = (lo + hi + 1) >> 1;
-						if(s.pix_prefix[mid] - base <= kGroupCap)
-							lo = mid;
-						else
-							hi = mid - 1;
-					}
-					p1 = lo;
+				int base = s.eff_prefix[p0];
+				int lo = p0 + 1, hi = min(p0 + kGroupPixels, 1024); // largest p1 within budget
+				while(lo < hi) {
+					int mid = (lo + hi + 1) >> 1;
+					if(s.eff_prefix[mid] - base <= kGroupBudget)
+						lo = mid;
+					else
+						hi = mid - 1;
 				}
-				s.group_end = p1;
+				s.group_end = lo;
+				s.kmin = 0xffffffffu;
+				s.kmax = 0u;
 			}
 			__syncthreads();
-			int p1 = s.group_end;
-			if(p1 < 0) {
-				p1 = -p1;
-				if(tid == 0) {
-					raiseError(p.info, LUCID_ERR_PIXEL_FRAGMENTS, uint32_t(bin), uint32_t(p0),
-							   uint32_t(s.pix_prefix[p0 + 1] - s.pix_prefix[p0]));
-					writePixel(p, bin_x + (p0 & 31), bin_y + (p0 >> 5), make_float4(1.0f, 0.0f, 0.0f, 1.0f));
-				}
-				__syncthreads();
-				p0 = p1;
-				continue;
-			}
+			const int p1 = s.group_end;
 			const int npix = p1 - p0;
-			const int gbase = s.pix_prefix[p0];
-			const int n = s.pix_prefix[p1] - gbase;
-			const int r0 = p0 >> 5, r1 = (p1 - 1) >> 5;
-
-			// C1. fragment generation
-			int running = 0;
-			for(int b = r0 >> 2; b <= (r1 >> 2); b++) {
-				int ne = s.band_count[b];
-				for(int base = 0; base < ne; base += RT) {
-					int j = base + tid;
-					int cnt = 0;
-					uint2 e = make_uint2(0, 0);
-					if(j < ne) {
-						e = scratch[size_t(b) * band_cap + j];
-#pragma unroll
-						for(int r = 0; r < 4; r++) {
-							int row = b * 4 + r;
-							if(row < r0 || row > r1)
-								continue;
-							int lo = (e.x >> (5 * r)) & 31, hi = (e.y >> (5 * r)) & 31;
-							int xlo = max(lo, p0 - 32 * row), xhi = min(hi, p1 - 1 - 32 * row);
-							cnt += max(0, xhi - xlo + 1);
-						}
-					}
-					int total;
-					int pos = blockExclusiveScan(cnt, s.scan_tmp, &total) + running;
-					if(cnt > 0) {
-						uint32_t tri = entryTri(e);
-						uint4 d = __ldg(p.tri_depth + tri);
-						float dx = bitsf(d.x), dy = bitsf(d.y), dz = bitsf(d.z);
-						uint32_t vbase = (uint32_t(b) << 8) | (uint32_t(j) << 11);
-#pragma unroll
-						for(int r = 0; r < 4; r++) {
-							int row = b * 4 + r;
-							if(row < r0 || row > r1)
-								continue;
-							int lo = (e.x >> (5 * r)) & 31, hi = (e.y >> (5 * r)) & 31;
-							int xlo = max(lo, p0 - 32 * row), xhi = min(hi, p1 - 1 - 32 * row);
-							float fy = float(bin_y + row);
-							float ty = dy * fy + dz;
-							for(int x = xlo; x <= xhi; x++) {
-								float inv_ray_pos = dx * float(bin_x + x) + ty;
-								if(pos < n) { // n <= kGroupCap; counts and spans agree by construction
-									s.kv[0][0][pos] = nearFirstKey(inv_ray_pos);
-									s.kv[0][1][pos] = vbase | uint32_t(row * 32 + x - p0);
-								}
-								pos++;
-							}
-						}
-					}
-					running += total;
-				}
-			}
-			__syncthreads();
-
-			// C2. stable radix sort: depth key bytes 0..3, then pixel
-			int cur = 0;
-			if(n > 1) {
-				for(int pass = 0; pass < 4; pass++)
-					if(radixPass(s, cur, n, pass * 8, false))
-						cur ^= 1;
-				if(radixPass(s, cur, n, 0, true))
-					cur ^= 1;
-			}
-			uint32_t* K = s.kv[cur][0];
-			uint32_t* V = s.kv[cur][1];
-
-			// C3. equal-depth runs in primitive order
-			for(int i = tid; i < n; i += RT) {
-				bool same_prev = i > 0 && K[i - 1] == K[i] && ((V[i - 1] ^ V[i]) & 0xffu) == 0;
-				bool same_next = i + 1 < n && K[i + 1] == K[i] && ((V[i + 1] ^ V[i]) & 0xffu) == 0;
-				if(!same_prev && same_next) {
-					int e = i + 1;
-					while(e < n && K[e] == K[i] && ((V[e] ^ V[i]) & 0xffu) == 0)
-						e++;
-					for(int a = i + 1; a < e; a++) { // insertion sort by primitive id
-						uint32_t va = V[a], pa = fragPrim(p, scratch, band_cap, va);
-						int c = a - 1;
-						while(c >= i && fragPrim(p, scratch, band_cap, V[c]) > pa) {
-							V[c + 1] = V[c];
-							c--;
-						}
-						V[c + 1] = va;
-					}
-				}
-			}
-			for(int t = tid; t < npix; t += RT) {
+			const int t = tid; // thread of pixel t (npix <= 256 < RT)
+			bool heavy = false;
+			if(t < npix) {
+				int c = s.pix_count[p0 + t];
+				heavy = c > kWindow;
 				s.px_T[t] = 1.0f;
 				s.px_c[t][0] = s.px_c[t][1] = s.px_c[t][2] = 0.0f;
-				s.px_cursor[t] = s.pix_prefix[p0 + t] - gbase;
+				s.px_lo[t] = 0;
+				s.px_done[t] = 0;
+				s.px_state[t] = c == 0 ? 1 : 0;
 			}
-			__syncthreads();
+			const bool windowed = __syncthreads_or(heavy);
 
-			// C4. shade in batches, blend sequentially per pixel
-			float4* stage = reinterpret_cast<float4*>(&s.kv[cur ^ 1][0][0]);
+			// C1. key range and per-pixel depth histograms of a heavy group
+			int nb_log = 0, shift = 0;
+			if(windowed) {
+				const int r0 = p0 >> 5, r1 = (p1 - 1) >> 5;
+				uint32_t kmn = 0xffffffffu, kmx = 0u;
+				for(int b = r0 >> 2; b <= (r1 >> 2); b++) {
+					const int ne = s.band_count[b];
+					for(int j = tid; j < ne; j += RT) {
+						uint2 e = scratch[size_t(b) * band_cap + j];
+						uint4 d = __ldg(p.tri_depth + entryTri(e));
+						float dx = bitsf(d.x), dy = bitsf(d.y), dz = bitsf(d.z);
+#pragma unroll
+						for(int r = 0; r < 4; r++) {
+							int row = b * 4 + r;
+							if(row < r0 || row > r1)
+								continue;
+							int lo = (e.x >> (5 * r)) & 31, hi = (e.y >> (5 * r)) & 31;
+							int xlo = max(lo, p0 - 32 * row), xhi = min(hi, p1 - 1 - 32 * row);
+							if(xlo > xhi)
+								continue;
+							// the evaluation is monotone in x, so the row's extremes are its ends
+							float ty = dy * float(bin_y + row) + dz;
+							uint32_t ka = nearFirstKey(dx * float(bin_x + xlo) + ty);
+							uint32_t kb = nearFirstKey(dx * float(bin_x + xhi) + ty);
+							kmn = min(kmn, min(ka, kb));
+							kmx = max(kmx, max(ka, kb));
+						}
+					}
+				}
+#pragma unroll
+				for(int o = 16; o > 0; o >>= 1) {
+					kmn = min(kmn, __shfl_xor_sync(0xffffffffu, kmn, o));
+					kmx = max(kmx, __shfl_xor_sync(0xffffffffu, kmx, o));
+				}
+				if(lane == 0) {
+					atomicMin(&s.kmin, kmn);
+					atomicMax(&s.kmax, kmx);
+				}
+				nb_log = 31 - __clz(max(1, min(256, kHistWords / npix))); // buckets per pixel = 2^nb_log
+				for(int i = tid; i < (npix << nb_log); i += RT)
+					s.hist[i] = 0;
+				__syncthreads();
+				const uint32_t kmin = s.kmin;
+				uint32_t range = s.kmax - kmin;
+				int bits = range ? 32 - __clz(range) : 0;
+				shift = max(0, bits - nb_log);
+				forEachGroupFragment(p, s, scratch, band_cap, bin_x, bin_y, p0, p1,
+									 [&](int tp, uint32_t key, int, int) {
+										 atomicAdd(&s.hist[(tp << nb_log) + int((key - kmin) >> shift)], 1u);
+									 });
+				__syncthreads();
+			}
+			RASTER_TIMER(2);
+			const int nbuckets = 1 << nb_log;
+			// fragments shaded per pixel per round: fewer pixels, deeper batches
+			const int batch = min(256, max(16, kStage / max(npix, 1)));
+
+			// C2. windows
 			while(true) {
-				for(int slot = tid; slot < npix * kShadeBatch; slot += RT) {
-					int t = slot / kShadeBatch, j = slot % kShadeBatch;
-					int f = s.px_cursor[t] + j;
-					int fend = s.pix_prefix[p0 + t + 1] - gbase;
-					if(f < fend && (s.px_T[t] != 0.0f || dump)) {
-						uint32_t v = V[f];
-						uint32_t band = (v >> 8) & 7u, eslot = v >> 11;
-						uint32_t tri = entryTri(scratch[size_t(band) * band_cap + eslot]);
-						int pl = p0 + int(v & 0xffu);
-						stage[slot] = shadeFragment(p, tri, keyToDepth(K[f]), bin_x + (pl & 31),
-													bin_y + (pl >> 5));
+				// this round's window of every active pixel
+				int wcount = 0;
+				if(t < npix && s.px_state[t] == 0) {
+					if(windowed) {
+						int c = s.px_lo[t];
+						int acc = s.hist[(t << nb_log) + c];
+						while(acc < kWindow && c + 1 < nbuckets) {
+							c++;
+							acc += s.hist[(t << nb_log) + c];
+						}
+						s.px_cut[t] = c;
+						wcount = acc;
+					} else {
+						s.px_cut[t] = 0;
+						wcount = s.pix_count[p0 + t];
+					}
+				}
+				int total;
+				int wbase = blockExclusiveScan(wcount, s.scan_tmp, &total);
+				if(total > kGroupCap) {
+					// defer the pixels that do not fit this round (their window stays)
+					bool fits = wbase + wcount <= kGroupCap;
+					if(!fits)
+						wcount = 0;
+					if(t < npix && s.px_state[t] == 0 && wbase == 0 && !fits) {
+						// the first pending pixel alone exceeds the capacity
+						raiseError(p.info, LUCID_ERR_PIXEL_FRAGMENTS, uint32_t(bin), uint32_t(p0 + t), uint32_t(total));
+						s.px_state[t] = 1;
+						s.px_T[t] = 0.0f;
+						s.px_c[t][0] = 1.0f, s.px_c[t][1] = 0.0f, s.px_c[t][2] = 0.0f;
+					}
+					wbase = blockExclusiveScan(wcount, s.scan_tmp, &total);
+				}
+				// sub-segments: one per pixel (light group) or one per bucket of the window; the
+				// bucket counts of the window become the sub-segment cursors
+				int nsmall = 0, nlarge = 0;
+				bool big = false;
+				if(t < npix) {
+					s.px_wbase[t] = wbase;
+					s.px_wend[t] = wbase;
+					s.px_bcur[t] = wbase;
+					s.px_wcnt[t] = wcount;
+					if(wcount == 0) {
+						s.px_cut[t] = -1; // not in this window (finished, empty or deferred)
+					} else if(windowed) {
+						int off = wbase;
+						for(int b = s.px_lo[t]; b <= s.px_cut[t]; b++) {
+							int c = int(s.hist[(t << nb_log) + b]);
+							s.hist[(t << nb_log) + b] = uint32_t(off);
+							off += c;
+							nsmall += c >= 2 && c <= 16;
+							nlarge += c > 16 && c <= 256;
+							big |= c > 256;
+						}
+					} else {
+						nsmall += wcount >= 2 && wcount <= 16;
+						nlarge += wcount > 16 && wcount <= 256;
+						big |= wcount > 256;
+					}
+				}
+				int small_off = blockExclusiveScan(nsmall, s.scan_tmp, (int*)nullptr);
+				int large_off = blockExclusiveScan(nlarge, s.scan_tmp, (int*)nullptr);
+				if(t < npix && (nsmall | nlarge)) {
+					const int wend = wbase + wcount;
+					auto add = [&](int beg, int c) {
+						if(c >= 2 && c <= 16)
+							s.sub_small[small_off++] = (uint32_t(beg) << 16) | uint32_t(c);
+						else if(c > 16 && c <= 256)
+							s.sub_large[large_off++] = (uint32_t(beg) << 16) | uint32_t(c);
+					};
+					if(windowed) {
+						const int lo = s.px_lo[t], cut = s.px_cut[t];
+						for(int b = lo; b <= cut; b++) {
+							int beg = int(s.hist[(t << nb_log) + b]);
+							int end = b < cut ? int(s.hist[(t << nb_log) + b + 1]) : wend;
+							add(beg, end - beg);
+						}
+					} else {
+						add(wbase, wcount);
+					}
+				}
+				if(t == npix - 1) { // the last pixel's cursors end at the list totals
+					s.n_small = small_off;
+					s.n_large = large_off;
+				}
+				const bool any_big = __syncthreads_or(big);
+				if(!__syncthreads_or(wcount > 0))
+					break;
+				const int n = total;
+
+				// C3. window fragments into their sub-segments
+				{
+					const uint32_t kmin = s.kmin;
+					forEachGroupFragment(p, s, scratch, band_cap, bin_x, bin_y, p0, p1,
+										 [&](int tp, uint32_t key, int b, int j) {
+											 if(s.px_cut[tp] < 0)
+												 return;
+											 int pos;
+											 if(windowed) {
+												 int bk = int((key - kmin) >> shift);
+												 if(bk < s.px_lo[tp] || bk > s.px_cut[tp])
+													 return;
+												 pos = int(atomicAdd(&s.hist[(tp << nb_log) + bk], 1u));
+											 } else {
+												 pos = atomicAdd(&s.px_wend[tp], 1);
+											 }
+											 if(pos < s.px_wbase[tp] + s.px_wcnt[tp]) {
+												 s.kv[0][0][pos] = key;
+												 s.kv[0][1][pos] = uint32_t(tp) | (uint32_t(b) << 8) | (uint32_t(j) << 11);
+											 }
+										 });
+				}
+				__syncthreads();
+				// every window segment must be exactly full (histogram and generation evaluate the
+				// same keys); anything else is an internal error
+				if(t < npix && s.px_cut[t] >= 0) {
+					int filled = windowed ? int(s.hist[(t << nb_log) + s.px_cut[t]]) : s.px_wend[t];
+					int want = s.px_wbase[t] + s.px_wcnt[t];
+					if(filled != want)
+						raiseError(p.info, LUCID_ERR_BIN_COUNT, uint32_t(bin), uint32_t(p0 + t),
+								   uint32_t(filled - s.px_wbase[t]));
+					s.px_wend[t] = want;
+				}
+				__syncthreads();
+				RASTER_TIMER(3);
+
+				// C4. sort every sub-segment by key: small ones by one thread, larger ones (<= 256)
+				// by one warp; any larger one sends the whole window to the block-wide radix sort
+				if(!any_big) {
+					uint32_t* K0 = s.kv[0][0];
+					uint32_t* V0 = s.kv[0][1];
+					const int ns = s.n_small, nl = s.n_large;
+					for(int i = tid; i < ns; i += RT) {
+						const uint32_t e = s.sub_small[i];
+						const int beg = int(e >> 16), cnt = int(e & 0xffffu);
+						if(cnt <= 2)
+							threadSortSegment<2>(K0, V0, beg, cnt);
+						else if(cnt <= 4)
+							threadSortSegment<4>(K0, V0, beg, cnt);
+						else if(cnt <= 8)
+							threadSortSegment<8>(K0, V0, beg, cnt);
+						else
+							threadSortSegment<16>(K0, V0, beg, cnt);
+					}
+					for(int i = warp; i < nl; i += NW) {
+						const uint32_t e = s.sub_large[i];
+						const int beg = int(e >> 16), cnt = int(e & 0xffffu);
+						if(cnt <= 32)
+							warpSortSegment<1>(K0, V0, beg, cnt);
+						else if(cnt <= 64)
+							warpSortSegment<2>(K0, V0, beg, cnt);
+						else if(cnt <= 128)
+							warpSortSegment<4>(K0, V0, beg, cnt);
+						else
+							warpSortSegment<8>(K0, V0, beg, cnt);
 					}
 				}
 				__syncthreads();
-				bool active = false;
-				for(int t = tid; t < npix; t += RT) {
-					int f = s.px_cursor[t];
-					int fend = s.pix_prefix[p0 + t + 1] - gbase;
-					int fbeg = s.pix_prefix[p0 + t] - gbase;
-					float T = s.px_T[t];
-					float c0 = s.px_c[t][0], c1 = s.px_c[t][1], c2 = s.px_c[t][2];
-					int j = 0;
-					for(; j < kShadeBatch && f < fend; j++, f++) {
-						if(T == 0.0f && !dump)
-							break;
-						float4 c = stage[t * kShadeBatch + j];
-						if(dump) {
-							int idx = f - fbeg;
-							if(idx < p.dump_max) {
-								int pl = p0 + t;
-								int px = bin_x + (pl & 31), py = bin_y + (pl >> 5);
-								if(px < p.width && py < p.height)
-									p.dump_prims[(size_t(py) * p.width + px) * p.dump_max + idx] =
-										int(fragPrim(p, scratch, band_cap, V[f]));
+				RASTER_TIMER(4);
+				const bool use_radix = any_big && n > 1;
+				if(tid == 0) {
+					atomicAdd((unsigned long long*)&p.info->raster_windows, 1ull);
+					atomicAdd((unsigned long long*)&p.info->raster_window_fragments, (unsigned long long)n);
+					if(use_radix)
+						atomicAdd(&p.info->raster_radix_windows, 1u);
+				}
+				int cur = 0;
+				if(use_radix) {
+					for(int pass = 0; pass < 4; pass++)
+						if(radixPass(s, cur, n, pass * 8, false))
+							cur ^= 1;
+					if(radixPass(s, cur, n, 0, true))
+						cur ^= 1;
+				}
+				uint32_t* K = s.kv[cur][0];
+				uint32_t* V = s.kv[cur][1];
+
+				// C5. equal-depth runs in primitive order
+				for(int i = tid; i < n; i += RT) {
+					bool same_prev = i > 0 && K[i - 1] == K[i] && ((V[i - 1] ^ V[i]) & 0xffu) == 0;
+					bool same_next = i + 1 < n && K[i + 1] == K[i] && ((V[i + 1] ^ V[i]) & 0xffu) == 0;
+					if(!same_prev && same_next) {
+						int e = i + 1;
+						while(e < n && K[e] == K[i] && ((V[e] ^ V[i]) & 0xffu) == 0)
+							e++;
+						for(int a = i + 1; a < e; a++) {
+							uint32_t va = V[a], pa = fragPrim(p, scratch, band_cap, va);
+							int c = a - 1;
+							while(c >= i && fragPrim(p, scratch, band_cap, V[c]) > pa) {
+								V[c + 1] = V[c];
+								c--;
 							}
-						}
-						if(additive) {
-							c0 = c0 + c.x * c.w;
-							c1 = c1 + c.y * c.w;
-							c2 = c2 + c.z * c.w;
-						} else {
-							c0 = c0 + (c.x * c.w) * T;
-							c1 = c1 + (c.y * c.w) * T;
-							c2 = c2 + (c.z * c.w) * T;
-							T = T * (1.0f - c.w);
-							if(alpha_threshold && T < (1.0f / 128.0f)) {
-								f = fend; // done with this pixel
-								break;
-							}
+							V[c + 1] = va;
 						}
 					}
-					s.px_cursor[t] = f;
-					s.px_T[t] = T;
-					s.px_c[t][0] = c0, s.px_c[t][1] = c1, s.px_c[t][2] = c2;
-					active |= f < fend && (T != 0.0f || dump);
 				}
-				if(!__syncthreads_or(active))
-					break;
+				__syncthreads();
+				RASTER_TIMER(1);
+
+				// C6. shade in batches, blend sequentially per pixel
+				float4* stage = reinterpret_cast<float4*>(&s.kv[cur ^ 1][0][0]);
+				while(true) {
+					for(int slot = tid; slot < npix * batch; slot += RT) {
+						int tp = slot / batch, j = slot - tp * batch;
+						int f = s.px_bcur[tp] + j;
+						if(f < s.px_wend[tp] && s.px_state[tp] == 0) {
+							uint32_t v = V[f];
+							uint32_t band = (v >> 8) & 7u, eslot = v >> 11;
+							uint32_t tri = entryTri(scratch[size_t(band) * band_cap + eslot]);
+							int pl = p0 + int(v & 0xffu);
+							stage[slot] = shadeFragment(p, tri, keyToDepth(K[f]), bin_x + (pl & 31),
+														bin_y + (pl >> 5));
+						}
+					}
+					__syncthreads();
+					RASTER_TIMER(5);
+					bool active = false;
+					if(t < npix && s.px_state[t] == 0) {
+						int f = s.px_bcur[t];
+						const int fend = s.px_wend[t], fbeg = s.px_wbase[t];
+						float T = s.px_T[t];
+						float c0 = s.px_c[t][0], c1 = s.px_c[t][1], c2 = s.px_c[t][2];
+						bool finished = false;
+						for(int j = 0; j < batch && f < fend; j++, f++) {
+							float4 c = stage[t * batch + j];
+							if(dump) {
+								int idx = s.px_done[t] + (f - fbeg);
+								if(idx < p.dump_max) {
+									int pl = p0 + t;
+									int px = bin_x + (pl & 31), py = bin_y + (pl >> 5);
+									if(px < p.width && py < p.height)
+										p.dump_prims[(size_t(py) * p.width + px) * p.dump_max + idx] =
+											int(fragPrim(p, scratch, band_cap, V[f]));
+								}
+							}
+							if(additive) {
+								c0 = c0 + c.x * c.w;
+								c1 = c1 + c.y * c.w;
+								c2 = c2 + c.z * c.w;
+							} else {
+								c0 = c0 + (c.x * c.w) * T;
+								c1 = c1 + (c.y * c.w) * T;
+								c2 = c2 + (c.z * c.w) * T;
+								T = T * (1.0f - c.w);
+								if((T == 0.0f && !dump) || (alpha_threshold && T < (1.0f / 128.0f))) {
+									finished = true;
+									f++;
+									break;
+								}
+							}
+						}
+						s.px_bcur[t] = f;
+						s.px_T[t] = T;
+						s.px_c[t][0] = c0, s.px_c[t][1] = c1, s.px_c[t][2] = c2;
+						if(finished)
+							s.px_state[t] = 1;
+						else
+							active = f < fend;
+					}
+					const bool any_active = __syncthreads_or(active);
+					RASTER_TIMER(6);
+					if(!any_active)
+						break;
+				}
+				// advance every pixel that took part in this window
+				if(t < npix && s.px_state[t] == 0 && s.px_cut[t] >= 0) {
+					s.px_done[t] += s.px_wcnt[t];
+					int next = s.px_cut[t] + 1;
+					s.px_lo[t] = next;
+					if(!windowed || next >= nbuckets)
+						s.px_state[t] = 1;
+				}
+				__syncthreads();
 			}
-			for(int t = tid; t < npix; t += RT) {
+
+			// C7. output
+			if(t < npix) {
 				int pl = p0 + t;
 				int px = bin_x + (pl & 31), py = bin_y + (pl >> 5);
 				float T = s.px_T[t];
@@ -559,14 +930,17 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(FrameParams p) {
 				o.w = 1.0f;
 				writePixel(p, px, py, o);
 				if(dump && px < p.width && py < p.height)
-					p.dump_counts[size_t(py) * p.width + px] = s.pix_prefix[pl + 1] - s.pix_prefix[pl];
+					p.dump_counts[size_t(py) * p.width + px] = s.pix_count[pl];
 			}
-			if(tid == 0 && running != n)
-				raiseError(p.info, LUCID_ERR_BIN_COUNT, uint32_t(bin), uint32_t(running), uint32_t(n));
 			__syncthreads();
+			RASTER_TIMER(7);
 			p0 = p1;
 		}
 	}
+	if(timers && tid == 0)
+		for(int i = 0; i < 8; i++)
+			atomicAdd(&p.info->raster_timers[i], uint32_t(tacc[i] >> 8));
+#undef RASTER_TIMER
 }
 
 void launchRaster(const FrameParams& p, int num_ctas, cudaStream_t stream) {

@@ -126,6 +126,33 @@ def test_many_layers_fragment_order(gpu, oracle):
     assert o["max_pixel_fragments"] > 100
 
 
+def test_depth_windows_early_exit(gpu, oracle):
+    """Hundreds of layers per pixel: per-pixel depth windows, stop at T == 0 (image only)."""
+    sc = scenes.random_tris(96, 64, 6000, seed=14, area_median=1500.0, area_sigma=0.4,
+                            alpha_range=(0.05, 0.5))
+    g, o = compare(sc, oracle)
+    assert o["max_pixel_fragments"] > 400
+
+
+def test_depth_windows_concentrated_depths(gpu, oracle):
+    """Most fragments of every pixel in one depth bucket: windows overshoot their target and
+    some pixels must wait for the next round (capacity deferral)."""
+    rng = np.random.default_rng(5)
+    tris, cols = [], []
+    for i in range(420):
+        d = 10.0 + 1e-4 * rng.random(3)
+        x0, y0 = rng.uniform(-20, 10, 2)
+        tris.append([(x0, y0, d[0]), (x0 + 120, y0 + 8, d[1]), (x0 + 10, y0 + 110, d[2])])
+        cols.append([(int(c[0]), int(c[1]), int(c[2]), 40) for c in rng.integers(0, 255, (3, 3))])
+    tris.append([(0, 0, 0.2), (96, 0, 0.21), (0, 64, 0.22)])
+    cols.append([(255, 0, 0, 10)] * 3)
+    tris.append([(96, 64, 99.0), (0, 64, 99.5), (96, 0, 98.0)])
+    cols.append([(0, 255, 0, 10)] * 3)
+    sc = scenes.screen_triangles(tris, cols, 96, 64)
+    compare(sc, oracle, dump=512)
+    compare(sc, oracle)
+
+
 def test_large_triangles_and_high_bins(gpu, oracle):
     sc = scenes.random_tris(200, 140, 3000, seed=4, area_median=2000.0, area_sigma=1.0,
                             large_fraction=0.05, large_area=(5000.0, 20000.0))
