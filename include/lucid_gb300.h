@@ -339,12 +339,24 @@ lucid_status lucid_raster_dump(lucid_renderer* renderer, const lucid_frame_input
 							   float* out_rgba, int32_t max_per_pixel, int32_t* host_counts,
 							   int32_t* host_prims, void* stream);
 
+/* Differentiable forward (no reference counterpart): lucid_render that also records each
+ * pixel's colour accumulated in FP64 and keeps the frame's bin lists for lucid_render_backward.
+ * out_rgba (device, width*height*4 floats) receives clamp(FP64 colour rounded to FP32) with
+ * alpha 1, the function whose gradient lucid_render_backward computes; it differs from
+ * lucid_render's FP32 blend by the FP32 rounding of that blend (~1e-6). Front-to-back blend
+ * only (LUCID_OPT_ADDITIVE_BLENDING and LUCID_OPT_ALPHA_THRESHOLD are rejected). */
+lucid_status lucid_render_forward_grad(lucid_renderer* renderer, const lucid_frame_inputs* inputs,
+									   float* out_rgba, void* stream);
+
 /* Backward pass (no reference counterpart): given dL/dimage (device, width*height*4 floats,
- * alpha channel ignored), accumulates dL/d(vertex RGBA) into dvertex_rgba (device,
- * num_verts*4 floats; only for LUCID_COLOR_RGBA32F colours) and dL/d(triangle opacity) into
- * dtri_opacity (device, num_quads*2 floats; requires inputs->tri_opacity). Either output may
- * be NULL. Gradients are ADDED to the buffers. Requires a prior lucid_render (or the full pass
- * sequence) of the same inputs on this renderer; fragment lists are recomputed, not stored. */
+ * alpha channel ignored) of the image of lucid_render_forward_grad, accumulates
+ * dL/d(vertex RGBA) into dvertex_rgba (device, num_verts*4 floats; LUCID_COLOR_RGBA32F
+ * colours only) and dL/d(triangle opacity) into dtri_opacity (device, num_quads*2 floats;
+ * requires inputs->tri_opacity). Either output may be NULL; gradients are ADDED. Channels whose
+ * unclamped colour lies outside [0, 1] pass no gradient. Positions are not differentiated.
+ * When the last pass on this renderer was lucid_render_forward_grad with an identical inputs
+ * struct and config (same pointers, contents unchanged since), its bin lists and per-pixel
+ * colours are reused; otherwise setup, binning and the FP64 colour pass are recomputed first. */
 lucid_status lucid_render_backward(lucid_renderer* renderer, const lucid_frame_inputs* inputs,
 								   const float* dl_dimage, float* dvertex_rgba,
 								   float* dtri_opacity, void* stream);

@@ -107,6 +107,7 @@ SIGNATURES = [
                                         ctypes.POINTER(c_size_t), c_void_p]),
     ("lucid_raster_dump", c_int32, [c_void_p, ctypes.POINTER(FrameInputsC), c_void_p, c_int32,
                                     c_void_p, c_void_p, c_void_p]),
+    ("lucid_render_forward_grad", c_int32, [c_void_p, ctypes.POINTER(FrameInputsC), c_void_p, c_void_p]),
     ("lucid_render_backward", c_int32, [c_void_p, ctypes.POINTER(FrameInputsC), c_void_p,
                                         c_void_p, c_void_p, c_void_p]),
     ("lucid_render_batch", c_int32, [c_void_p, ctypes.POINTER(ViewC), c_int32, c_void_p]),

@@ -71,7 +71,18 @@ struct FrameParams {
 	int* dump_counts;     // verification mode (may be null)
 	int* dump_prims;
 	int dump_max;
+	// gradient passes (kRasterStats / kRasterBackward)
+	double* px_color64;   // per pixel: FP64 unclamped colour (3 doubles, stats pass output)
+	float* px_color32;    // per pixel: FP32 unclamped colour (3 floats, clamp mask)
+	const float* dl_dimage;
+	float* dvertex_rgba;
+	float* dtri_opacity;
 };
+
+// Raster kernel modes.
+constexpr int kRasterForward = 0;  // image
+constexpr int kRasterStats = 1;    // image + per-pixel FP64 colour for the backward pass
+constexpr int kRasterBackward = 2; // gradients of vertex RGBA / triangle opacity
 
 // Offsets into the per-bin counter array (definitions.glsl:117-129)
 __device__ __forceinline__ uint32_t& binQuadCounts(const FrameParams& p, int i) { return p.counts[p.bin_count * 0 + i]; }

@@ -92,6 +92,16 @@ struct lucid_renderer {
 	FrameParams last{}; // parameters of the last quad setup (used by the later passes)
 	bool have_frame = false;
 
+	// gradient pass state, allocated on the first lucid_render_forward_grad / _backward
+	double* px_color64 = nullptr;
+	float* px_color32 = nullptr;
+	float* stats_image = nullptr;
+	// set by lucid_render_forward_grad, cleared by every other pass: the bin lists and the
+	// per-pixel colours then belong to grad_inputs / grad_config
+	bool grad_ready = false;
+	lucid_frame_inputs grad_inputs{};
+	lucid_config grad_config{};
+
 	size_t infoBytes() const { return sizeof(lucid_info) + size_t(10) * bin_count * 4; }
 	lucid_info* info() const { return reinterpret_cast<lucid_info*>(info_block); }
 	uint32_t* counts() const { return reinterpret_cast<uint32_t*>(info_block + sizeof(lucid_info)); }
@@ -455,6 +465,7 @@ extern "C" lucid_status lucid_quad_setup(lucid_renderer* r, const lucid_frame_in
 	LUCID_CUDA_TRY(cudaMemsetAsync(r->info_block, 0, r->infoBytes(), s));
 	r->last = makeParams(r, in, nullptr);
 	r->have_frame = true;
+	r->grad_ready = false;
 	launchSetup(r->last, s);
 	return checkLaunch("quad setup");
 }
@@ -489,6 +500,7 @@ static lucid_status rasterImpl(lucid_renderer* r, const lucid_frame_inputs* in, 
 	lucid_status st = validateInputs(r, in);
 	if(st != LUCID_OK)
 		return st;
+	r->grad_ready = false;
 	FrameParams p = r->last;
 	p.colors = in->colors;
 	p.color_format = in->color_format;
@@ -611,11 +623,90 @@ extern "C" lucid_status lucid_raster_dump(lucid_renderer* r, const lucid_frame_i
 	return st;
 }
 
+namespace {
+
+lucid_status checkGradInputs(lucid_renderer* r, const lucid_frame_inputs* in) {
+	lucid_status st = validateInputs(r, in);
+	if(st != LUCID_OK)
+		return st;
+	if(r->opts.flags & (LUCID_OPT_ADDITIVE_BLENDING | LUCID_OPT_ALPHA_THRESHOLD))
+		return fail(LUCID_NOT_SUPPORTED, "gradient passes support the front-to-back blend only");
+	if(!r->px_color64) {
+		const size_t npix = size_t(r->width) * r->height;
+		if((st = allocate(r, &r->px_color64, npix * 3)) != LUCID_OK ||
+		   (st = allocate(r, &r->px_color32, npix * 3)) != LUCID_OK ||
+		   (st = allocate(r, &r->stats_image, npix * 4)) != LUCID_OK)
+			return st;
+	}
+	return LUCID_OK;
+}
+
+// setup, binning and the stats raster pass (image + per-pixel FP64 colour)
+lucid_status gradForward(lucid_renderer* r, const lucid_frame_inputs* in, float* out, void* stream) {
+	lucid_status st;
+	if((st = lucid_quad_setup(r, in, stream)) != LUCID_OK || (st = lucid_bin_count(r, stream)) != LUCID_OK ||
+	   (st = lucid_bin_categorize(r, stream)) != LUCID_OK || (st = lucid_bin_dispatch(r, stream)) != LUCID_OK)
+		return st;
+	cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+	FrameParams p = r->last;
+	p.out_rgba = out;
+	p.px_color64 = r->px_color64;
+	p.px_color32 = r->px_color32;
+	if((st = resetRasterCounters(r, s)) != LUCID_OK)
+		return st;
+	launchRaster(p, r->raster_ctas, s, kRasterStats);
+	if((st = checkLaunch("raster (stats)")) != LUCID_OK)
+		return st;
+	r->grad_ready = true;
+	r->grad_inputs = *in;
+	r->grad_config = *in->config;
+	return LUCID_OK;
+}
+
+} // namespace
+
+extern "C" lucid_status lucid_render_forward_grad(lucid_renderer* r, const lucid_frame_inputs* in,
+												  float* out_rgba, void* stream) {
+	if(!r || !out_rgba)
+		return fail(LUCID_INVALID_ARG, "lucid_render_forward_grad: renderer and out_rgba are required");
+	lucid_status st = checkGradInputs(r, in);
+	if(st != LUCID_OK)
+		return st;
+	return gradForward(r, in, out_rgba, stream);
+}
+
 extern "C" lucid_status lucid_render_backward(lucid_renderer* r, const lucid_frame_inputs* in,
 											  const float* dl_dimage, float* dvertex_rgba,
 											  float* dtri_opacity, void* stream) {
-	(void)r, (void)in, (void)dl_dimage, (void)dvertex_rgba, (void)dtri_opacity, (void)stream;
-	return fail(LUCID_NOT_SUPPORTED, "lucid_render_backward is not built yet");
+	if(!r || !dl_dimage)
+		return fail(LUCID_INVALID_ARG, "lucid_render_backward: renderer and dl_dimage are required");
+	lucid_status st = checkGradInputs(r, in);
+	if(st != LUCID_OK)
+		return st;
+	if(dvertex_rgba && in->color_format != LUCID_COLOR_RGBA32F)
+		return fail(LUCID_INVALID_ARG, "vertex colour gradients need LUCID_COLOR_RGBA32F colours");
+	if(dtri_opacity && !in->tri_opacity)
+		return fail(LUCID_INVALID_ARG, "opacity gradients need inputs->tri_opacity");
+	// Reuse the forward pass's bin lists and per-pixel colours when the last pass on this
+	// renderer was lucid_render_forward_grad of the same inputs; otherwise recompute them.
+	lucid_frame_inputs cmp = *in;
+	cmp.config = r->grad_inputs.config; // the config is compared by contents
+	const bool reuse = r->grad_ready && memcmp(&r->grad_inputs, &cmp, sizeof(cmp)) == 0 &&
+					   memcmp(&r->grad_config, in->config, sizeof(lucid_config)) == 0;
+	if(!reuse && (st = gradForward(r, in, r->stats_image, stream)) != LUCID_OK)
+		return st;
+	cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+	FrameParams p = r->last;
+	p.out_rgba = r->stats_image;
+	p.px_color64 = r->px_color64;
+	p.px_color32 = r->px_color32;
+	p.dl_dimage = dl_dimage;
+	p.dvertex_rgba = dvertex_rgba;
+	p.dtri_opacity = dtri_opacity;
+	if((st = resetRasterCounters(r, s)) != LUCID_OK)
+		return st;
+	launchRaster(p, r->raster_ctas, s, kRasterBackward);
+	return checkLaunch("raster (backward)");
 }
 
 extern "C" lucid_status lucid_render_batch(lucid_renderer* r, const lucid_view* views,

@@ -139,6 +139,78 @@ __device__ __forceinline__ float4 shadeFragment(const FrameParams& p, uint32_t t
 	return col;
 }
 
+// shadeFragment with everything the backward pass needs to route gradients to the vertex
+// colours and the triangle opacity (same float operations, so the same colour).
+struct FragmentShade {
+	float4 col;           // colour used by the blend (alpha includes the opacity)
+	float4 inst;          // instance colour factor
+	float wgt[3];         // barycentric weights of the three vertices
+	uint32_t vid[3];      // vertex ids
+	float opacity;        // per-triangle opacity factor (1 if none)
+	float alpha_pre;      // alpha before the opacity factor
+	uint32_t prim;
+	bool has_vc;
+};
+
+__device__ __forceinline__ FragmentShade shadeFragmentFull(const FrameParams& p, uint32_t tri,
+														   float inv_ray_pos, int px, int py) {
+	FragmentShade f;
+	uint4 b0r = __ldg(p.tri_bary + size_t(tri) * 2);
+	uint4 b1r = __ldg(p.tri_bary + size_t(tri) * 2 + 1);
+	uint32_t fid = __ldg(&p.tri_depth[tri].w);
+	float fx = float(px), fy = float(py);
+	float ray_pos = 1.0f / inv_ray_pos;
+	float e0 = bitsf(b0r.x) * fx + (bitsf(b0r.y) * fy + bitsf(b0r.z));
+	float e1 = bitsf(b1r.x) * fx + (bitsf(b1r.y) * fy + bitsf(b1r.z));
+	float b0 = e0 * ray_pos, b1 = e1 * ray_pos;
+	b0 = b0 - bitsf(b0r.w);
+	b1 = b1 - bitsf(b1r.w);
+	uint32_t flags = fid & 0xffffu, inst = fid >> 16;
+	f.inst = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+	if((flags & LUCID_INST_HAS_COLOR) && p.instance_colors)
+		f.inst = decodeRGBA8(__ldg(p.instance_colors + inst));
+	f.col = f.inst;
+	float w = (1.0f - b0) - b1;
+	f.wgt[0] = w, f.wgt[1] = b0, f.wgt[2] = b1;
+	uint32_t quad = tri >> 1, second = tri & 1;
+	uint4 qv = __ldg(p.quad_verts + quad);
+	f.vid[0] = qv.x, f.vid[1] = second ? qv.z : qv.y, f.vid[2] = second ? qv.w : qv.z;
+	f.has_vc = (flags & LUCID_INST_HAS_VERTEX_COLORS) != 0;
+	if(f.has_vc) {
+		float4 c0, c1, c2;
+		if(p.color_format == LUCID_COLOR_RGBA8) {
+			uint4 qc = __ldg(p.quad_colors + quad);
+			c0 = decodeRGBA8(qc.x);
+			c1 = decodeRGBA8(second ? qc.z : qc.y);
+			c2 = decodeRGBA8(second ? qc.w : qc.z);
+		} else if(p.color_format == LUCID_COLOR_RGBA16F) {
+			const uint2* hc = reinterpret_cast<const uint2*>(p.colors);
+			uint2 h0 = __ldg(hc + f.vid[0]), h1 = __ldg(hc + f.vid[1]), h2 = __ldg(hc + f.vid[2]);
+			auto cvt = [](uint2 h) {
+				__half2 a = *reinterpret_cast<__half2*>(&h.x), b = *reinterpret_cast<__half2*>(&h.y);
+				float2 fa = __half22float2(a), fb = __half22float2(b);
+				return make_float4(fa.x, fa.y, fb.x, fb.y);
+			};
+			c0 = cvt(h0), c1 = cvt(h1), c2 = cvt(h2);
+		} else {
+			const float4* fc = reinterpret_cast<const float4*>(p.colors);
+			c0 = __ldg(fc + f.vid[0]), c1 = __ldg(fc + f.vid[1]), c2 = __ldg(fc + f.vid[2]);
+		}
+		f.col.x = f.col.x * (w * c0.x + (b0 * c1.x + b1 * c2.x));
+		f.col.y = f.col.y * (w * c0.y + (b0 * c1.y + b1 * c2.y));
+		f.col.z = f.col.z * (w * c0.z + (b0 * c1.z + b1 * c2.z));
+		f.col.w = f.col.w * (w * c0.w + (b0 * c1.w + b1 * c2.w));
+	}
+	f.alpha_pre = f.col.w;
+	f.opacity = 1.0f;
+	f.prim = __ldg(p.quad_source + quad) * 2 + second;
+	if(p.tri_opacity) {
+		f.opacity = __ldg(p.tri_opacity + f.prim);
+		f.col.w = f.col.w * f.opacity;
+	}
+	return f;
+}
+
 __device__ __forceinline__ uint32_t fragPrim(const FrameParams& p, const uint2* scratch, int band_cap,
 											 uint32_t val) {
 	uint32_t band = (val >> 8) & 7u, slot = val >> 11;
@@ -365,6 +437,7 @@ __device__ __forceinline__ void forEachGroupFragment(const FrameParams& p, const
 			dx = bitsf(d.x), dy = bitsf(d.y), dz = bitsf(d.z);
 		}
 		const int cnt = min(32, jend - j0);
+#pragma unroll 4
 		for(int k = 0; k < cnt; k++) {
 			uint32_t ex = __shfl_sync(0xffffffffu, e.x, k), ey = __shfl_sync(0xffffffffu, e.y, k);
 			int lo = (ex >> rshift) & 31, hi = (ey >> rshift) & 31;
@@ -383,6 +456,7 @@ __device__ __forceinline__ void forEachGroupFragment(const FrameParams& p, const
 	}
 }
 
+template <int MODE>
 __global__ void __launch_bounds__(RT, 1) rasterKernel(FrameParams p) {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	RasterSmem& s = *reinterpret_cast<RasterSmem*>(smem_raw);
@@ -572,6 +646,9 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(FrameParams p) {
 			const int p1 = s.group_end;
 			const int npix = p1 - p0;
 			const int t = tid; // thread of pixel t (npix <= 256 < RT)
+			// gradient passes: per-pixel state kept in the registers of thread t
+			double acc64[3] = {0.0, 0.0, 0.0}, c64[3] = {0.0, 0.0, 0.0}, T64 = 1.0;
+			float grad[3] = {0.0f, 0.0f, 0.0f};
 			bool heavy = false;
 			if(t < npix) {
 				int c = s.pix_count[p0 + t];
@@ -581,6 +658,25 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(FrameParams p) {
 				s.px_lo[t] = 0;
 				s.px_done[t] = 0;
 				s.px_state[t] = c == 0 ? 1 : 0;
+				if constexpr(MODE == kRasterBackward) {
+					// dL/dout through the clamp of the forward output (gradient passes where
+					// 0 <= C <= 1), and the FP64 colour of the stats pass
+					int pl = p0 + t;
+					int px = bin_x + (pl & 31), py = bin_y + (pl >> 5);
+					bool any = false;
+					if(px < p.width && py < p.height) {
+						size_t pix = size_t(py) * p.width + px;
+						for(int ch = 0; ch < 3; ch++) {
+							float cf = p.px_color32[pix * 3 + ch];
+							float gch = p.dl_dimage[pix * 4 + ch];
+							grad[ch] = (cf >= 0.0f && cf <= 1.0f) ? gch : 0.0f;
+							c64[ch] = p.px_color64[pix * 3 + ch];
+							any |= grad[ch] != 0.0f;
+						}
+					}
+					if(!any)
+						s.px_state[t] = 1;
+				}
 			}
 			const bool windowed = __syncthreads_or(heavy);
 
@@ -845,16 +941,19 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(FrameParams p) {
 				// C6. shade in batches, blend sequentially per pixel
 				float4* stage = reinterpret_cast<float4*>(&s.kv[cur ^ 1][0][0]);
 				while(true) {
-					for(int slot = tid; slot < npix * batch; slot += RT) {
-						int tp = slot / batch, j = slot - tp * batch;
-						int f = s.px_bcur[tp] + j;
-						if(f < s.px_wend[tp] && s.px_state[tp] == 0) {
-							uint32_t v = V[f];
-							uint32_t band = (v >> 8) & 7u, eslot = v >> 11;
-							uint32_t tri = entryTri(scratch[size_t(band) * band_cap + eslot]);
-							int pl = p0 + int(v & 0xffu);
-							stage[slot] = shadeFragment(p, tri, keyToDepth(K[f]), bin_x + (pl & 31),
-														bin_y + (pl >> 5));
+					if constexpr(MODE != kRasterBackward) {
+#pragma unroll 2
+						for(int slot = tid; slot < npix * batch; slot += RT) {
+							int tp = slot / batch, j = slot - tp * batch;
+							int f = s.px_bcur[tp] + j;
+							if(f < s.px_wend[tp] && s.px_state[tp] == 0) {
+								uint32_t v = V[f];
+								uint32_t band = (v >> 8) & 7u, eslot = v >> 11;
+								uint32_t tri = entryTri(scratch[size_t(band) * band_cap + eslot]);
+								int pl = p0 + int(v & 0xffu);
+								stage[slot] = shadeFragment(p, tri, keyToDepth(K[f]), bin_x + (pl & 31),
+															bin_y + (pl >> 5));
+							}
 						}
 					}
 					__syncthreads();
@@ -867,7 +966,57 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(FrameParams p) {
 						float c0 = s.px_c[t][0], c1 = s.px_c[t][1], c2 = s.px_c[t][2];
 						bool finished = false;
 						for(int j = 0; j < batch && f < fend; j++, f++) {
-							float4 c = stage[t * batch + j];
+							float4 c;
+							if constexpr(MODE == kRasterBackward) {
+								// recompute the fragment's shading and route dL/dC to its inputs:
+								// dC/dc = a*T, dC/da = c*T - S/(1-a) with S the colour behind it,
+								// S = C - (colour accumulated up to and including it) in FP64
+								uint32_t v = V[f];
+								uint32_t band = (v >> 8) & 7u, eslot = v >> 11;
+								uint32_t tri = entryTri(scratch[size_t(band) * band_cap + eslot]);
+								int pl = p0 + t;
+								FragmentShade fs = shadeFragmentFull(p, tri, keyToDepth(K[f]),
+																	 bin_x + (pl & 31), bin_y + (pl >> 5));
+								c = fs.col;
+								// the gradient terms use an FP64 transmittance (the FP32 one of
+								// the image drifts by ~n ulp and c - B cancels)
+								const float a = c.w;
+								const float ca[3] = {c.x * a, c.y * a, c.z * a};
+								const float cc[3] = {c.x, c.y, c.z};
+								double da = 0.0;
+								float dc[3];
+								const double inv = 1.0 - double(a);
+								for(int ch = 0; ch < 3; ch++) {
+									acc64[ch] += double(ca[ch]) * T64;
+									double behind = c64[ch] - acc64[ch];
+									dc[ch] = float(double(grad[ch]) * double(a) * T64);
+									double term = double(cc[ch]) * T64;
+									if(inv != 0.0)
+										term -= behind / inv;
+									da += double(grad[ch]) * term;
+								}
+								T64 *= inv;
+								if(p.dvertex_rgba && fs.has_vc && p.color_format == LUCID_COLOR_RGBA32F) {
+									const float inst[4] = {fs.inst.x, fs.inst.y, fs.inst.z, fs.inst.w};
+									const float dalpha = float(da) * fs.opacity;
+									for(int k = 0; k < 3; k++) {
+										float* dst = p.dvertex_rgba + size_t(fs.vid[k]) * 4;
+										for(int ch = 0; ch < 3; ch++)
+											atomicAdd(dst + ch, inst[ch] * fs.wgt[k] * dc[ch]);
+										atomicAdd(dst + 3, inst[3] * fs.wgt[k] * dalpha);
+									}
+								}
+								if(p.dtri_opacity && p.tri_opacity)
+									atomicAdd(p.dtri_opacity + fs.prim, float(da) * fs.alpha_pre);
+							} else {
+								c = stage[t * batch + j];
+							}
+							if constexpr(MODE == kRasterStats) {
+								acc64[0] += double(c.x * c.w) * T64;
+								acc64[1] += double(c.y * c.w) * T64;
+								acc64[2] += double(c.z * c.w) * T64;
+								T64 *= 1.0 - double(c.w);
+							}
 							if(dump) {
 								int idx = s.px_done[t] + (f - fbeg);
 								if(idx < p.dump_max) {
@@ -919,18 +1068,37 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(FrameParams p) {
 			}
 
 			// C7. output
-			if(t < npix) {
+			if(t < npix && MODE != kRasterBackward) {
 				int pl = p0 + t;
 				int px = bin_x + (pl & 31), py = bin_y + (pl >> 5);
 				float T = s.px_T[t];
+				float un[3] = {s.px_c[t][0] + T * bg.x, s.px_c[t][1] + T * bg.y, s.px_c[t][2] + T * bg.z};
+				if constexpr(MODE == kRasterStats) {
+					// the differentiable forward returns the FP64 colour rounded to FP32, the
+					// function whose gradient the backward pass computes
+					const float bgc[3] = {bg.x, bg.y, bg.z};
+					for(int ch = 0; ch < 3; ch++) {
+						acc64[ch] += T64 * double(bgc[ch]);
+						un[ch] = float(acc64[ch]);
+					}
+				}
 				float4 o;
-				o.x = fminf(fmaxf(s.px_c[t][0] + T * bg.x, 0.0f), 1.0f);
-				o.y = fminf(fmaxf(s.px_c[t][1] + T * bg.y, 0.0f), 1.0f);
-				o.z = fminf(fmaxf(s.px_c[t][2] + T * bg.z, 0.0f), 1.0f);
+				o.x = fminf(fmaxf(un[0], 0.0f), 1.0f);
+				o.y = fminf(fmaxf(un[1], 0.0f), 1.0f);
+				o.z = fminf(fmaxf(un[2], 0.0f), 1.0f);
 				o.w = 1.0f;
 				writePixel(p, px, py, o);
 				if(dump && px < p.width && py < p.height)
 					p.dump_counts[size_t(py) * p.width + px] = s.pix_count[pl];
+				if constexpr(MODE == kRasterStats) {
+					if(px < p.width && py < p.height) {
+						size_t pix = size_t(py) * p.width + px;
+						for(int ch = 0; ch < 3; ch++) {
+							p.px_color64[pix * 3 + ch] = acc64[ch];
+							p.px_color32[pix * 3 + ch] = un[ch];
+						}
+					}
+				}
 			}
 			__syncthreads();
 			RASTER_TIMER(7);
@@ -943,13 +1111,25 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(FrameParams p) {
 #undef RASTER_TIMER
 }
 
-void launchRaster(const FrameParams& p, int num_ctas, cudaStream_t stream) {
-	rasterKernel<<<num_ctas, RT, sizeof(RasterSmem), stream>>>(p);
+void launchRaster(const FrameParams& p, int num_ctas, cudaStream_t stream, int mode) {
+	if(mode == kRasterStats)
+		rasterKernel<kRasterStats><<<num_ctas, RT, sizeof(RasterSmem), stream>>>(p);
+	else if(mode == kRasterBackward)
+		rasterKernel<kRasterBackward><<<num_ctas, RT, sizeof(RasterSmem), stream>>>(p);
+	else
+		rasterKernel<kRasterForward><<<num_ctas, RT, sizeof(RasterSmem), stream>>>(p);
 }
 
 cudaError_t configureRasterKernel() {
-	return cudaFuncSetAttribute(rasterKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-								int(sizeof(RasterSmem)));
+	cudaError_t err;
+	if((err = cudaFuncSetAttribute(rasterKernel<kRasterForward>,
+								   cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(RasterSmem)))) != cudaSuccess)
+		return err;
+	if((err = cudaFuncSetAttribute(rasterKernel<kRasterStats>,
+								   cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(RasterSmem)))) != cudaSuccess)
+		return err;
+	return cudaFuncSetAttribute(rasterKernel<kRasterBackward>,
+								cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(RasterSmem)));
 }
 
 } // namespace lucid

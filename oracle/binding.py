@@ -138,3 +138,91 @@ def run(scene, max_visible_quads: int | None = None, raster: bool = True, image6
         num_hblock_tris=int(outs.num_hblock_tris),
         max_pixel_fragments=int(outs.max_pixel_fragments), max_visible_quads=mvq)
     return out
+
+
+class GradModel:
+    """FP64 gradient model of a scene (see oracle_grad_* in lucid_oracle.h)."""
+
+    def __init__(self, scene, max_visible_quads=None):
+        L = lib()
+        if not hasattr(L, "_grad_bound"):
+            L.oracle_grad_build.argtypes = [ctypes.POINTER(OracleInputs)]
+            L.oracle_grad_build.restype = ctypes.c_void_p
+            L.oracle_grad_free.argtypes = [ctypes.c_void_p]
+            L.oracle_grad_loss.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+            L.oracle_grad_loss.restype = ctypes.c_double
+            L.oracle_grad_analytic.argtypes = [ctypes.c_void_p] + [ctypes.c_void_p] * 5
+            L.oracle_grad_backprop.argtypes = [ctypes.c_void_p] + [ctypes.c_void_p] * 6
+            L.oracle_grad_fd.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                         ctypes.c_int, ctypes.c_int, ctypes.c_double]
+            L.oracle_grad_fd.restype = ctypes.c_double
+            L.oracle_grad_num_fragments.argtypes = [ctypes.c_void_p]
+            L.oracle_grad_num_fragments.restype = ctypes.c_uint64
+            L._grad_bound = True
+        self.L = L
+        self.scene = scene
+        mvq = max_visible_quads or max(1024, scene.num_quads)
+        self._keep = dict(
+            positions=np.ascontiguousarray(scene.positions, np.float32),
+            colors=np.ascontiguousarray(scene.colors),
+            quads=np.ascontiguousarray(scene.quads, np.uint32),
+            inst=np.ascontiguousarray(scene.instances, np.int32),
+            icol=np.ascontiguousarray(scene.instance_colors, np.uint32),
+            opac=None if scene.tri_opacity is None else np.ascontiguousarray(scene.tri_opacity, np.float32))
+        k = self._keep
+        ins = OracleInputs(
+            width=scene.width, height=scene.height, max_visible_quads=mvq, low_high_threshold=1024,
+            flags=0, order_mode=0, positions=_ptr(k["positions"]), colors=_ptr(k["colors"]),
+            color_format=scene.color_format, num_verts=k["positions"].shape[0], quads_ib=_ptr(k["quads"]),
+            num_quads=k["quads"].shape[0], num_instances=k["inst"].shape[0], instances=_ptr(k["inst"]),
+            instance_colors=_ptr(k["icol"]), tri_opacity=_ptr(k["opac"]), config=ctypes.addressof(scene.config),
+            bin_subset=None, num_bin_subset=0, num_threads=1)
+        self.ctx = L.oracle_grad_build(ctypes.byref(ins))
+        if not self.ctx:
+            raise RuntimeError("oracle_grad_build failed")
+
+    def __del__(self):
+        if getattr(self, "ctx", None):
+            self.L.oracle_grad_free(self.ctx)
+            self.ctx = None
+
+    @property
+    def num_fragments(self):
+        return int(self.L.oracle_grad_num_fragments(self.ctx))
+
+    def loss(self, vcolors, opacity, target):
+        vc = np.ascontiguousarray(vcolors, np.float64)
+        op = None if opacity is None else np.ascontiguousarray(opacity, np.float64)
+        tg = np.ascontiguousarray(target, np.float32)
+        return float(self.L.oracle_grad_loss(self.ctx, vc.ctypes.data, _ptr(op), tg.ctypes.data))
+
+    def analytic(self, vcolors, opacity, target):
+        vc = np.ascontiguousarray(vcolors, np.float64)
+        op = None if opacity is None else np.ascontiguousarray(opacity, np.float64)
+        tg = np.ascontiguousarray(target, np.float32)
+        dvc = np.zeros_like(vc)
+        dop = None if op is None else np.zeros_like(op)
+        self.L.oracle_grad_analytic(self.ctx, vc.ctypes.data, _ptr(op), tg.ctypes.data, dvc.ctypes.data,
+                                    _ptr(dop))
+        return dvc, dop
+
+    def backprop(self, vcolors, opacity, dl_dimage, color32):
+        """Adjoint alone: dL/dparams for a given upstream gradient dl_dimage [h, w, 4] and the
+        FP32 unclamped colour color32 [h, w, 3] (clamp mask)."""
+        vc = np.ascontiguousarray(vcolors, np.float64)
+        op = None if opacity is None else np.ascontiguousarray(opacity, np.float64)
+        gi = np.ascontiguousarray(dl_dimage, np.float32)
+        c32 = np.ascontiguousarray(color32, np.float32)
+        dvc = np.zeros_like(vc)
+        dop = None if op is None else np.zeros_like(op)
+        rc = self.L.oracle_grad_backprop(self.ctx, vc.ctypes.data, _ptr(op), gi.ctypes.data, c32.ctypes.data,
+                                         dvc.ctypes.data, _ptr(dop))
+        if rc != 0:
+            raise RuntimeError("oracle_grad_backprop failed")
+        return dvc, dop
+
+    def fd(self, vcolors, opacity, target, kind, index, h=1e-4):
+        vc = np.ascontiguousarray(vcolors, np.float64)
+        op = None if opacity is None else np.ascontiguousarray(opacity, np.float64)
+        tg = np.ascontiguousarray(target, np.float32)
+        return float(self.L.oracle_grad_fd(self.ctx, vc.ctypes.data, _ptr(op), tg.ctypes.data, kind, index, h))

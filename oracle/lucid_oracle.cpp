@@ -677,9 +677,10 @@ void shadeFragment(const State& s, const Frag& f, int px, int py, float col[4]) 
 		col[3] = col[3] * in->tri_opacity[f.prim];
 }
 
-void rasterBin(const State& s, int bin, oracle_outputs* out, std::vector<std::vector<Frag>>& px,
-			   uint64_t& nfrag, uint64_t& nhbt, uint32_t& maxfrag) {
-	const oracle_inputs* in = s.in;
+// Fragments of every pixel of one bin (row-major 32x32 lists, unsorted); returns the count of
+// (tri, half-block) pairs with a covered pixel.
+uint64_t binFragments(const State& s, int bin, std::vector<std::vector<Frag>>& px) {
+	uint64_t nhbt = 0;
 	int bx = bin % s.bcx, by = bin / s.bcx;
 	int bin_x = bx * kBinSize, bin_y = by * kBinSize;
 	for(auto& v : px)
@@ -722,6 +723,20 @@ void rasterBin(const State& s, int bin, oracle_outputs* out, std::vector<std::ve
 			nhbt += __builtin_popcount(colmask);
 		}
 	}
+	return nhbt;
+}
+
+// Exact per-pixel order: nearest first (larger inv_ray_pos), ties by input primitive id.
+inline bool fragLess(const Frag& a, const Frag& b) {
+	return a.key != b.key ? a.key < b.key : a.prim < b.prim;
+}
+
+void rasterBin(const State& s, int bin, oracle_outputs* out, std::vector<std::vector<Frag>>& px,
+			   uint64_t& nfrag, uint64_t& nhbt, uint32_t& maxfrag) {
+	const oracle_inputs* in = s.in;
+	int bx = bin % s.bcx, by = bin / s.bcx;
+	int bin_x = bx * kBinSize, bin_y = by * kBinSize;
+	nhbt += binFragments(s, bin, px);
 	const float* bg = in->config->background_color;
 	bool additive = (in->flags & LUCID_OPT_ADDITIVE_BLENDING) != 0;
 	bool alpha_threshold = (in->flags & LUCID_OPT_ALPHA_THRESHOLD) != 0;
@@ -734,9 +749,7 @@ void rasterBin(const State& s, int bin, oracle_outputs* out, std::vector<std::ve
 			if(pxx >= s.w)
 				break;
 			auto& fr = px[r * 32 + x];
-			std::sort(fr.begin(), fr.end(), [](const Frag& a, const Frag& b) {
-				return a.key != b.key ? a.key < b.key : a.prim < b.prim;
-			});
+			std::sort(fr.begin(), fr.end(), fragLess);
 			nfrag += fr.size();
 			maxfrag = std::max(maxfrag, uint32_t(fr.size()));
 			size_t pix = size_t(py) * s.w + pxx;
@@ -828,17 +841,7 @@ void raster(State& s, oracle_outputs* out) {
 	}
 }
 
-} // namespace
-
-extern "C" int oracle_version(void) { return 1; }
-
-extern "C" int oracle_run(const oracle_inputs* in, oracle_outputs* out) {
-	if(!in || !out || !in->config || in->width <= 0 || in->height <= 0 ||
-	   in->max_visible_quads <= 0 || in->order_mode != 0)
-		return 1;
-	if(in->num_quads > 0 && (!in->positions || !in->quads_ib || !in->instances))
-		return 1;
-	State s;
+void initState(State& s, const oracle_inputs* in) {
 	s.in = in;
 	s.w = in->width, s.h = in->height;
 	s.bcx = (s.w + kBinSize - 1) / kBinSize;
@@ -853,6 +856,263 @@ extern "C" int oracle_run(const oracle_inputs* in, oracle_outputs* out) {
 	// quad_setup.glsl:397-398: ray through the centre of pixel (0, 0)
 	V3 dxy = add(s.dirx, s.diry);
 	s.ray_dir0 = add(s.dir0, mul(dxy, 0.5f));
+}
+
+// ---------------------------------------------------------------------------------------------
+// FP64 gradient model. Positions are frozen, so coverage, per-pixel order and the barycentric
+// weights (computed in FP32 exactly as the shader does, shading.glsl:116-133) are constants;
+// colours and alphas are FP64 functions of the vertex colours and triangle opacities.
+
+struct GFrag {
+	uint32_t vid[3];
+	uint32_t prim;
+	double wgt[3];
+	double inst[4];
+	bool has_vc;
+};
+
+struct GradCtx {
+	int w, h;
+	double bg[3];
+	bool has_opacity;
+	std::vector<uint32_t> pix_off; // fragments of pixel i: [pix_off[i], pix_off[i+1])
+	std::vector<GFrag> frags;
+	std::vector<std::vector<uint32_t>> vert_pixels, prim_pixels;
+};
+
+void pixelColor64(const GradCtx& g, uint32_t pix, const double* vc, const double* op, double C[3]) {
+	double T = 1.0;
+	C[0] = C[1] = C[2] = 0.0;
+	for(uint32_t i = g.pix_off[pix]; i < g.pix_off[pix + 1]; i++) {
+		const GFrag& f = g.frags[i];
+		double col[4] = {f.inst[0], f.inst[1], f.inst[2], f.inst[3]};
+		if(f.has_vc)
+			for(int ch = 0; ch < 4; ch++)
+				col[ch] *= f.wgt[0] * vc[size_t(f.vid[0]) * 4 + ch] + f.wgt[1] * vc[size_t(f.vid[1]) * 4 + ch] +
+						   f.wgt[2] * vc[size_t(f.vid[2]) * 4 + ch];
+		double a = col[3] * (op ? op[f.prim] : 1.0);
+		for(int ch = 0; ch < 3; ch++)
+			C[ch] += col[ch] * a * T;
+		T *= 1.0 - a;
+	}
+	for(int ch = 0; ch < 3; ch++)
+		C[ch] += T * g.bg[ch];
+}
+
+double pixelLoss64(const GradCtx& g, uint32_t pix, const double* vc, const double* op, const float* target) {
+	double C[3];
+	pixelColor64(g, pix, vc, op, C);
+	double l = 0.0;
+	for(int ch = 0; ch < 3; ch++) {
+		double d = std::min(std::max(C[ch], 0.0), 1.0) - double(target[size_t(pix) * 4 + ch]);
+		l += d * d;
+	}
+	return l;
+}
+
+} // namespace
+
+extern "C" int oracle_version(void) { return 1; }
+
+extern "C" void* oracle_grad_build(const oracle_inputs* in) {
+	if(!in || !in->config || in->order_mode != 0)
+		return nullptr;
+	State s;
+	initState(s, in);
+	oracle_outputs dummy;
+	memset(&dummy, 0, sizeof(dummy));
+	quadSetup(s, &dummy);
+	binning(s, &dummy);
+	GradCtx* g = new GradCtx();
+	g->w = s.w, g->h = s.h;
+	for(int ch = 0; ch < 3; ch++)
+		g->bg[ch] = in->config->background_color[ch];
+	g->has_opacity = in->tri_opacity != nullptr;
+	const size_t npix = size_t(s.w) * s.h;
+	std::vector<std::vector<GFrag>> per_pix(npix);
+	std::vector<std::vector<Frag>> px(1024);
+	for(int bin = 0; bin < s.bins; bin++) {
+		binFragments(s, bin, px);
+		int bin_x = (bin % s.bcx) * kBinSize, bin_y = (bin / s.bcx) * kBinSize;
+		for(int i = 0; i < 1024; i++) {
+			auto& fr = px[i];
+			if(fr.empty())
+				continue;
+			std::sort(fr.begin(), fr.end(), fragLess);
+			int pxx = bin_x + (i & 31), py = bin_y + (i >> 5);
+			auto& out = per_pix[size_t(py) * s.w + pxx];
+			for(const Frag& f : fr) {
+				// barycentric weights exactly as shadeFragment computes them
+				const uint32_t* d = &s.tri_depth[size_t(f.tri) * 4];
+				const uint32_t* b = &s.tri_bary[size_t(f.tri) * 8];
+				float fx = float(pxx), fy = float(py);
+				float ray_pos = 1.0f / f.depth;
+				float e0 = bitsf(b[0]) * fx + (bitsf(b[1]) * fy + bitsf(b[2]));
+				float e1 = bitsf(b[4]) * fx + (bitsf(b[5]) * fy + bitsf(b[6]));
+				float b0 = e0 * ray_pos - bitsf(b[3]), b1 = e1 * ray_pos - bitsf(b[7]);
+				float wgt = (1.0f - b0) - b1;
+				uint32_t flags = d[3] & 0xffffu, inst = d[3] >> 16;
+				uint32_t quad = f.tri >> 1, second = f.tri & 1;
+				GFrag gf;
+				gf.vid[0] = s.quad_verts[size_t(quad) * 4];
+				gf.vid[1] = s.quad_verts[size_t(quad) * 4 + 1 + second];
+				gf.vid[2] = s.quad_verts[size_t(quad) * 4 + 2 + second];
+				gf.prim = f.prim;
+				gf.wgt[0] = wgt, gf.wgt[1] = b0, gf.wgt[2] = b1;
+				float ic[4] = {1.0f, 1.0f, 1.0f, 1.0f};
+				if((flags & LUCID_INST_HAS_COLOR) && in->instance_colors)
+					decodeRGBA8(in->instance_colors[inst], ic);
+				for(int ch = 0; ch < 4; ch++)
+					gf.inst[ch] = ic[ch];
+				gf.has_vc = (flags & LUCID_INST_HAS_VERTEX_COLORS) != 0;
+				out.push_back(gf);
+			}
+		}
+	}
+	g->pix_off.resize(npix + 1, 0);
+	for(size_t i = 0; i < npix; i++)
+		g->pix_off[i + 1] = g->pix_off[i] + uint32_t(per_pix[i].size());
+	g->frags.reserve(g->pix_off[npix]);
+	g->vert_pixels.assign(size_t(in->num_verts), {});
+	g->prim_pixels.assign(size_t(in->num_quads) * 2, {});
+	for(size_t i = 0; i < npix; i++) {
+		for(const GFrag& f : per_pix[i]) {
+			g->frags.push_back(f);
+			for(int k = 0; k < 3; k++)
+				if(g->vert_pixels[f.vid[k]].empty() || g->vert_pixels[f.vid[k]].back() != i)
+					g->vert_pixels[f.vid[k]].push_back(uint32_t(i));
+			if(f.prim < g->prim_pixels.size())
+				g->prim_pixels[f.prim].push_back(uint32_t(i));
+		}
+		std::vector<GFrag>().swap(per_pix[i]);
+	}
+	return g;
+}
+
+extern "C" void oracle_grad_free(void* ctx) { delete static_cast<GradCtx*>(ctx); }
+
+extern "C" uint64_t oracle_grad_num_fragments(void* ctx) {
+	return static_cast<GradCtx*>(ctx)->frags.size();
+}
+
+extern "C" double oracle_grad_loss(void* ctx, const double* vc, const double* op, const float* target) {
+	const GradCtx& g = *static_cast<GradCtx*>(ctx);
+	double l = 0.0;
+	for(uint32_t i = 0; i + 1 < g.pix_off.size(); i++)
+		l += pixelLoss64(g, i, vc, g.has_opacity ? op : nullptr, target);
+	return l;
+}
+
+namespace {
+// Backpropagates per-pixel upstream gradients through the FP64 blend. With target != NULL the
+// upstream gradient is that of the squared-error loss on the FP64 colour; otherwise it is
+// dl_dimage (h*w*4 floats), masked where color32 (h*w*3 floats, the unclamped colour of the
+// FP32 forward pass) lies outside [0, 1].
+int gradBackprop(const GradCtx& g, const double* vc, const double* op, const float* target,
+				 const float* dl_dimage, const float* color32, double* dvc, double* dop) {
+	const double* opp = g.has_opacity ? op : nullptr;
+	std::vector<double> col, alpha, T;
+	for(uint32_t pix = 0; pix + 1 < g.pix_off.size(); pix++) {
+		uint32_t beg = g.pix_off[pix], end = g.pix_off[pix + 1];
+		if(beg == end)
+			continue;
+		size_t n = end - beg;
+		col.resize(n * 4), alpha.resize(n), T.resize(n + 1);
+		double C[3] = {0.0, 0.0, 0.0};
+		T[0] = 1.0;
+		for(size_t i = 0; i < n; i++) {
+			const GFrag& f = g.frags[beg + i];
+			for(int ch = 0; ch < 4; ch++) {
+				double v = f.inst[ch];
+				if(f.has_vc)
+					v *= f.wgt[0] * vc[size_t(f.vid[0]) * 4 + ch] + f.wgt[1] * vc[size_t(f.vid[1]) * 4 + ch] +
+						 f.wgt[2] * vc[size_t(f.vid[2]) * 4 + ch];
+				col[i * 4 + ch] = v;
+			}
+			alpha[i] = col[i * 4 + 3] * (opp ? opp[f.prim] : 1.0);
+			for(int ch = 0; ch < 3; ch++)
+				C[ch] += col[i * 4 + ch] * alpha[i] * T[i];
+			T[i + 1] = T[i] * (1.0 - alpha[i]);
+		}
+		double gch[3];
+		for(int ch = 0; ch < 3; ch++) {
+			C[ch] += T[n] * g.bg[ch];
+			double out = std::min(std::max(C[ch], 0.0), 1.0);
+			// torch-style clamp gradient: passes where min <= C <= max
+			if(target)
+				gch[ch] = (C[ch] >= 0.0 && C[ch] <= 1.0) ? 2.0 * (out - double(target[size_t(pix) * 4 + ch])) : 0.0;
+			else {
+				float cf = color32[size_t(pix) * 3 + ch];
+				gch[ch] = (cf >= 0.0f && cf <= 1.0f) ? double(dl_dimage[size_t(pix) * 4 + ch]) : 0.0;
+			}
+		}
+		// back to front: B = colour behind fragment i+1; dC/da_i = T_i (c_i - B)
+		double B[3] = {g.bg[0], g.bg[1], g.bg[2]};
+		for(size_t ii = n; ii-- > 0;) {
+			const GFrag& f = g.frags[beg + ii];
+			double dcol[4] = {0.0, 0.0, 0.0, 0.0}, da = 0.0;
+			for(int ch = 0; ch < 3; ch++) {
+				dcol[ch] = gch[ch] * alpha[ii] * T[ii];
+				da += gch[ch] * T[ii] * (col[ii * 4 + ch] - B[ch]);
+			}
+			double opv = opp ? opp[f.prim] : 1.0;
+			dcol[3] = da * opv;
+			if(dvc && f.has_vc)
+				for(int k = 0; k < 3; k++)
+					for(int ch = 0; ch < 4; ch++)
+						dvc[size_t(f.vid[k]) * 4 + ch] += f.inst[ch] * f.wgt[k] * dcol[ch];
+			if(dop && opp)
+				dop[f.prim] += da * col[ii * 4 + 3];
+			for(int ch = 0; ch < 3; ch++)
+				B[ch] = col[ii * 4 + ch] * alpha[ii] + (1.0 - alpha[ii]) * B[ch];
+		}
+	}
+	return 0;
+}
+} // namespace
+
+extern "C" int oracle_grad_analytic(void* ctx, const double* vc, const double* op, const float* target,
+									double* dvc, double* dop) {
+	const GradCtx& g = *static_cast<GradCtx*>(ctx);
+	return gradBackprop(g, vc, g.has_opacity ? op : nullptr, target, nullptr, nullptr, dvc, dop);
+}
+
+extern "C" int oracle_grad_backprop(void* ctx, const double* vc, const double* op, const float* dl_dimage,
+									const float* color32, double* dvc, double* dop) {
+	const GradCtx& g = *static_cast<GradCtx*>(ctx);
+	if(!dl_dimage || !color32)
+		return 1;
+	return gradBackprop(g, vc, g.has_opacity ? op : nullptr, nullptr, dl_dimage, color32, dvc, dop);
+}
+
+extern "C" double oracle_grad_fd(void* ctx, const double* vc, const double* op, const float* target,
+								 int kind, int index, double h) {
+	const GradCtx& g = *static_cast<GradCtx*>(ctx);
+	const std::vector<uint32_t>& pixels = kind == 0 ? g.vert_pixels[size_t(index) / 4] : g.prim_pixels[index];
+	std::vector<double> v(vc, vc + g.vert_pixels.size() * 4);
+	std::vector<double> o;
+	if(g.has_opacity)
+		o.assign(op, op + g.prim_pixels.size());
+	double* param = kind == 0 ? &v[index] : &o[index];
+	const double x = *param;
+	double lp = 0.0, lm = 0.0;
+	*param = x + h;
+	for(uint32_t pix : pixels)
+		lp += pixelLoss64(g, pix, v.data(), g.has_opacity ? o.data() : nullptr, target);
+	*param = x - h;
+	for(uint32_t pix : pixels)
+		lm += pixelLoss64(g, pix, v.data(), g.has_opacity ? o.data() : nullptr, target);
+	return (lp - lm) / (2.0 * h);
+}
+
+extern "C" int oracle_run(const oracle_inputs* in, oracle_outputs* out) {
+	if(!in || !out || !in->config || in->width <= 0 || in->height <= 0 ||
+	   in->max_visible_quads <= 0 || in->order_mode != 0)
+		return 1;
+	if(in->num_quads > 0 && (!in->positions || !in->quads_ib || !in->instances))
+		return 1;
+	State s;
+	initState(s, in);
 	out->error_code = 0;
 	quadSetup(s, out);
 	binning(s, out);

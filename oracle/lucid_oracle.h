@@ -88,9 +88,31 @@ typedef struct oracle_outputs {
  * Returns 0 on success, nonzero on invalid arguments. */
 int oracle_run(const oracle_inputs* in, oracle_outputs* out);
 
-/* Per-bin statistics of the binning result, used by scene reports: number of tris per bin
- * (2*quads + tris) written into out[bin_count]. */
 int oracle_version(void);
+
+/* ---- FP64 gradient model (checker of lucid_render_backward) ----
+ * Builds the exact per-pixel fragment lists of the scene (coverage, order and barycentric
+ * weights depend on positions only, which stay frozen) and evaluates, in FP64, the loss
+ * L = sum over pixels and RGB of (clamp(C) - target)^2 as a function of the per-vertex RGBA
+ * colours (num_verts*4 doubles) and the per-triangle opacities (num_quads*2 doubles, or NULL
+ * when the scene has none). target: h*w*4 floats (alpha ignored). */
+void* oracle_grad_build(const oracle_inputs* in);
+void oracle_grad_free(void* ctx);
+double oracle_grad_loss(void* ctx, const double* vcolors, const double* opacity, const float* target);
+/* analytic gradient (back-to-front recursion in FP64); outputs may be NULL */
+int oracle_grad_analytic(void* ctx, const double* vcolors, const double* opacity, const float* target,
+						 double* dvcolors, double* dopacity);
+/* adjoint alone: backpropagates a given upstream gradient dl_dimage (h*w*4 floats, alpha
+ * ignored) through the FP64 blend; channels whose FP32 unclamped colour color32 (h*w*3 floats)
+ * lies outside [0, 1] pass no gradient (the clamp) */
+int oracle_grad_backprop(void* ctx, const double* vcolors, const double* opacity, const float* dl_dimage,
+						 const float* color32, double* dvcolors, double* dopacity);
+/* central difference (L(x+h) - L(x-h)) / 2h of one parameter: kind 0 = vertex colour
+ * component index (vertex*4 + channel), kind 1 = triangle opacity index; only the pixels the
+ * parameter touches are re-evaluated */
+double oracle_grad_fd(void* ctx, const double* vcolors, const double* opacity, const float* target,
+					  int kind, int index, double h);
+uint64_t oracle_grad_num_fragments(void* ctx);
 
 #ifdef __cplusplus
 }
