@@ -199,6 +199,128 @@ def run_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
+def grad_bench(steps, warmup, flush_buf):
+    """Forward+backward on grad512 (512x512, 200k triangles, FP32 vertex RGBA, per-triangle
+    opacity): L2 loss to a target rendered from perturbed colours, gradients with respect to
+    vertex RGBA and triangle opacity. Times the plain forward (lucid_render), the differentiable
+    forward (lucid_render_forward_grad), and forward_grad + loss gradient + lucid_render_backward."""
+    import torch
+    from lucid_gb300 import scenes
+    from lucid_gb300._lib import check
+    from lucid_gb300.renderer import FrameInputs, LucidRenderer, _dptr, _stream_ptr
+    import ctypes
+    sc = scenes.workload("grad512")
+    r = LucidRenderer(sc.width, sc.height, max_input_quads=sc.num_quads, max_visible_quads=sc.num_quads,
+                      max_bin_refs=8 * sc.num_quads)
+    frame = FrameInputs.from_scene(sc)
+    rng = np.random.default_rng(104)
+    pert = sc.colors.copy()
+    pert[:, :3] = np.clip(pert[:, :3] + rng.normal(0, 0.1, size=pert[:, :3].shape), 0, 1)
+    tframe = FrameInputs.from_scene(scenes.Scene(**{**sc.__dict__, "colors": pert.astype(np.float32)}))
+    target = r.render(tframe)
+    img = r.new_image()
+    dvc = torch.zeros_like(frame.colors)
+    dop = torch.zeros_like(frame.tri_opacity)
+    stream = torch.cuda.current_stream()
+    fi = frame.c_struct()
+
+    def fwd_plain():
+        r.render(frame, img)
+
+    def fwd_grad():
+        check(r.lib.lucid_render_forward_grad(r.handle, ctypes.byref(fi), _dptr(img), _stream_ptr()),
+              "lucid_render_forward_grad")
+
+    def fwd_bwd():
+        fwd_grad()
+        g = 2.0 * (img - target)
+        g[..., 3] = 0.0
+        check(r.lib.lucid_render_backward(r.handle, ctypes.byref(fi), _dptr(g), _dptr(dvc), _dptr(dop),
+                                          _stream_ptr()), "lucid_render_backward")
+
+    def timed(fn):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        ms = []
+        for i in range(steps):
+            flush_buf.fill_(i & 0xFF)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return float(np.median(ms))
+
+    t_plain, t_fgrad, t_fb = timed(fwd_plain), timed(fwd_grad), timed(fwd_bwd)
+    info, _ = r.info()
+    r.close()
+    return {"workload": "grad512: 512x512, 200k random triangles (cpu720 distributions), FP32 vertex "
+                        "RGBA, triangle opacity U[0.1,0.9], L2 loss to a perturbed-colour target",
+            "fwd_ms": t_plain, "fwd_grad_ms": t_fgrad, "fwd_bwd_ms": t_fb, "ratio": t_fb / t_plain,
+            "fragments": int(info.num_fragments), "median_of": steps}
+
+
+def batch_bench(steps, warmup, flush_buf, num_views=64):
+    """Batched multi-view frames: num_views random-triangle views (cpu720 distributions) with
+    resolutions drawn from {256^2, 512^2, 1280x720, 1920x1080} and log-uniform [10k, 500k]
+    triangles, rendered by one lucid_render_batch (replay of its recorded graph) against
+    num_views sequential lucid_render calls (one renderer per resolution) on the same GPU."""
+    import torch
+    from lucid_gb300 import scenes
+    from lucid_gb300.renderer import FrameInputs, LucidRenderer
+    views = scenes.batch_views(num_views)
+    frames = [(FrameInputs.from_scene(v), v.width, v.height) for v in views]
+    outs = [torch.empty((v.height, v.width, 4), dtype=torch.float32, device="cuda") for v in views]
+    total_quads = sum(max(1, v.num_quads) for v in views)
+    plain = {}
+    for v in views:
+        key = (v.width, v.height)
+        if key not in plain:
+            nq = max(x.num_quads for x in views if (x.width, x.height) == key)
+            plain[key] = LucidRenderer(v.width, v.height, max_input_quads=nq, max_visible_quads=nq,
+                                       max_bin_refs=8 * nq)
+    br = LucidRenderer(max(v.width for v in views), max(v.height for v in views), max_input_quads=total_quads,
+                       max_visible_quads=total_quads, max_bin_refs=4 * total_quads, max_views=num_views)
+    stream = torch.cuda.current_stream()
+
+    def run_plain():
+        for (f, w, h), o in zip(frames, outs):
+            plain[(w, h)].render(f, o)
+
+    def run_batch():
+        br.render_batch(frames, outs=outs)
+
+    def timed(fn):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        ms = []
+        for i in range(steps):
+            flush_buf.fill_(i & 0xFF)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return float(np.median(ms))
+
+    t_plain = timed(run_plain)
+    t_batch = timed(run_batch)
+    frags = sum(int(br.batch_info(i).num_fragments) for i in range(num_views))
+    errors = [i for i in range(num_views) if br.batch_info(i).error_code != 0]
+    for r in list(plain.values()) + [br]:
+        r.close()
+    return {"workload": f"{num_views} views, resolutions from {{256^2, 512^2, 1280x720, 1920x1080}}, "
+                        "log-uniform [10k, 500k] random triangles each (cpu720 distributions)",
+            "views": num_views, "triangles": int(sum(v.num_tris for v in views)), "fragments": frags,
+            "plain_ms": t_plain, "batch_ms": t_batch, "plain_frames_per_s": num_views / (t_plain / 1e3),
+            "batch_frames_per_s": num_views / (t_batch / 1e3), "speedup": t_plain / t_batch,
+            "view_errors": errors, "median_of": steps}
+
+
 def main():
     args = parse_args()
     rank, world, local = dist_setup(args.gpus)
@@ -318,6 +440,10 @@ def main():
     e2e_ms = e0.elapsed_time(e1) / args.steps
     e2e_value = fragments * world / (e2e_ms / 1e3)
 
+    # ---- forward+backward workload (rank 0 only)
+    fwd_bwd = grad_bench(max(5, args.steps), max(3, args.warmup), flush_buf) if rank == 0 else None
+    batch = batch_bench(max(5, args.steps), max(3, args.warmup), flush_buf) if rank == 0 else None
+
     # ---- CPU baseline (rank 0, N=1 only)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -352,6 +478,8 @@ def main():
             "clocks": clocks.summary(),
             "gpu_launches": KERNELS_PER_FRAME * args.steps,
             "mtri_per_s": scene.num_tris * args.steps * world / (total_ms / 1e3) / 1e6,
+            "fwd_bwd": fwd_bwd,
+            "batch": batch,
         }
         print(json.dumps(line), flush=True)
     r.close()

@@ -210,7 +210,10 @@ typedef struct lucid_options {
 	int32_t binning_ctas;      /* CTAs of bin_count / bin_dispatch (0 = 2 per SM)              */
 	int32_t raster_ctas_per_sm;/* 0 = as many as fit                                           */
 	int32_t max_views;         /* views of lucid_render_batch                                  */
-	int32_t reserved[5];
+	int32_t grad_store_fragments; /* fragment store of lucid_render_forward_grad: 0 = grows on
+	                               * demand, > 0 = fixed capacity, < 0 = none (the backward pass
+	                               * recomputes the fragment lists instead of reading them)      */
+	int32_t reserved[4];
 } lucid_options;
 
 /* ---------------------------------------------------------------------------------------- */
@@ -350,8 +353,8 @@ lucid_status lucid_render_forward_grad(lucid_renderer* renderer, const lucid_fra
 
 /* Backward pass (no reference counterpart): given dL/dimage (device, width*height*4 floats,
  * alpha channel ignored) of the image of lucid_render_forward_grad, accumulates
- * dL/d(vertex RGBA) into dvertex_rgba (device, num_verts*4 floats; LUCID_COLOR_RGBA32F
- * colours only) and dL/d(triangle opacity) into dtri_opacity (device, num_quads*2 floats;
+ * dL/d(vertex RGBA) into dvertex_rgba (device, num_verts*4 floats, 16-byte aligned;
+ * LUCID_COLOR_RGBA32F colours only) and dL/d(triangle opacity) into dtri_opacity (device, num_quads*2 floats;
  * requires inputs->tri_opacity). Either output may be NULL; gradients are ADDED. Channels whose
  * unclamped colour lies outside [0, 1] pass no gradient. Positions are not differentiated.
  * When the last pass on this renderer was lucid_render_forward_grad with an identical inputs
@@ -362,11 +365,23 @@ lucid_status lucid_render_backward(lucid_renderer* renderer, const lucid_frame_i
 								   float* dtri_opacity, void* stream);
 
 /* Batched forward (no reference counterpart): renders num_views independent views (each with
- * its own size, geometry and config) with one launch per pass for all views. The renderer must
- * have been created with options.max_views >= num_views and width/height at least as large as
- * every view. views is a HOST array. */
+ * its own size, geometry, colour format and config) with one launch per pass for all views:
+ * setup and binning kernels whose CTA ranges map to views, and one persistent raster kernel
+ * over the bins of every view (HIGH bins of all views first). Each view's image is bit-identical
+ * to lucid_render of that view alone. views is a HOST array; num_views <= options.max_views
+ * (at most 256); every view fits the renderer's width/height; the views' input quads together
+ * fit options.max_visible_quads and max_input_quads; their bin references share
+ * options.max_bin_refs. The frame is recorded once per batch topology (view count, sizes, quad
+ * and instance counts) as a CUDA graph and replayed by later calls: the first call of a new
+ * topology synchronises `stream` and allocates; later calls only stage changed view parameters
+ * (pointers, configs) and launch the graph. Input contents may change freely between calls.
+ * Must not be called while `stream` is being captured. Not re-entrant across streams.
+ * Per-view device statistics and errors: lucid_get_batch_info. */
 lucid_status lucid_render_batch(lucid_renderer* renderer, const lucid_view* views,
 								int32_t num_views, void* stream);
+
+/* Copies (synchronising `stream`) the lucid_info of view `view` of the last lucid_render_batch. */
+lucid_status lucid_get_batch_info(lucid_renderer* renderer, int32_t view, lucid_info* out, void* stream);
 
 /* Picks raster launch parameters by timing candidate configurations on `inputs`; stores the
  * winner in the renderer and returns it in *out_ctas_per_sm / *out_low_high_threshold. */

@@ -35,7 +35,7 @@ class Options(ctypes.Structure):
                 ("low_high_threshold", c_int32), ("max_bin_refs", c_int32),
                 ("band_capacity", c_int32), ("binning_ctas", c_int32),
                 ("raster_ctas_per_sm", c_int32), ("max_views", c_int32),
-                ("reserved", c_int32 * 5)]
+                ("grad_store_fragments", c_int32), ("reserved", c_int32 * 4)]
 
 
 class FrameInputsC(ctypes.Structure):
@@ -111,6 +111,7 @@ SIGNATURES = [
     ("lucid_render_backward", c_int32, [c_void_p, ctypes.POINTER(FrameInputsC), c_void_p,
                                         c_void_p, c_void_p, c_void_p]),
     ("lucid_render_batch", c_int32, [c_void_p, ctypes.POINTER(ViewC), c_int32, c_void_p]),
+    ("lucid_get_batch_info", c_int32, [c_void_p, c_int32, ctypes.POINTER(Info), c_void_p]),
     ("lucid_autotune", c_int32, [c_void_p, ctypes.POINTER(FrameInputsC), c_void_p,
                                  ctypes.POINTER(c_int32), ctypes.POINTER(c_int32), c_void_p]),
     ("lucid_bin_noalloc", c_int32, [c_void_p, c_void_p, c_int32, c_int32, c_int32, c_int32,

@@ -58,26 +58,28 @@ __device__ __forceinline__ void scanlineStep(BinScan& s, int& bmin, int& bmax) {
 	bmax = f2i(xmax) >> kBinShift;
 }
 
-__device__ __forceinline__ void ctaRange(int n, int& beg, int& end) {
-	beg = int((int64_t(n) * blockIdx.x) / gridDim.x);
-	end = int((int64_t(n) * (blockIdx.x + 1)) / gridDim.x);
+__device__ __forceinline__ void ctaRange(int n, int cta, int ncta, int& beg, int& end) {
+	beg = int((int64_t(n) * cta) / ncta);
+	end = int((int64_t(n) * (cta + 1)) / ncta);
 }
 
 // ---------------------------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(kBinningThreads, 1) binCountKernel(FrameParams p) {
+template <class Src> __global__ void __launch_bounds__(kBinningThreads, 1) binCountKernel(Src src) {
 	extern __shared__ int s_bins[];
+	int cta, ncta;
+	const FrameParams& p = src.get(cta, ncta);
 	const int bins = p.bin_count, bcx = p.bin_count_x, bcy = p.bin_count_y;
 	const int mvq = p.max_visible_quads;
 	const int nsmall = p.info->num_visible_quads[0], nlarge = p.info->num_visible_quads[1];
-	int* hist = p.bin_batches + size_t(blockIdx.x) * 2 * bins;
+	int* hist = p.bin_batches + size_t(cta) * 2 * bins;
 
 	// ---- small quads: every bin of the AABB (bin_counter.glsl:64-80)
 	for(int i = threadIdx.x; i < bins; i += blockDim.x)
 		s_bins[i] = 0;
 	__syncthreads();
 	int sbeg, send;
-	ctaRange(nsmall, sbeg, send);
+	ctaRange(nsmall, cta, ncta, sbeg, send);
 	for(int k = sbeg + threadIdx.x; k < send; k += blockDim.x) {
 		int x0, y0, x1, y1;
 		decodeAABB28(p.quad_aabbs[k], x0, y0, x1, y1);
@@ -99,7 +101,7 @@ __global__ void __launch_bounds__(kBinningThreads, 1) binCountKernel(FrameParams
 		s_bins[i] = 0;
 	__syncthreads();
 	int lbeg, lend;
-	ctaRange(nlarge, lbeg, lend);
+	ctaRange(nlarge, cta, ncta, lbeg, lend);
 	int items = 2 * (lend - lbeg);
 	for(int it = threadIdx.x; it < items; it += blockDim.x) {
 		int k = lbeg + (it >> 1), second = it & 1;
@@ -147,13 +149,13 @@ __global__ void __launch_bounds__(kBinningThreads, 1) binCountKernel(FrameParams
 		if(v > 0)
 			atomicAdd(&binTriCounts(p, i), uint32_t(v));
 	}
-	if(threadIdx.x < 2 && blockIdx.x < LUCID_INFO_MAX_DISPATCHES) {
+	if(threadIdx.x < 2 && cta < LUCID_INFO_MAX_DISPATCHES) {
 		int batch = threadIdx.x == 0 ? 4096 : 512;
 		int beg = threadIdx.x == 0 ? sbeg : lbeg, end = threadIdx.x == 0 ? send : lend;
-		p.info->dispatcher_first_batch[threadIdx.x][blockIdx.x] = end > beg ? beg / batch : -1;
-		p.info->dispatcher_num_batches[threadIdx.x][blockIdx.x] = (end - beg + batch - 1) / batch;
+		p.info->dispatcher_first_batch[threadIdx.x][cta] = end > beg ? beg / batch : -1;
+		p.info->dispatcher_num_batches[threadIdx.x][cta] = (end - beg + batch - 1) / batch;
 	}
-	if(blockIdx.x == 0 && threadIdx.x == 0) {
+	if(cta == 0 && threadIdx.x == 0) {
 		// quad_setup.glsl:471-485
 		int tasks = (nsmall + 4095) / 4096 + (nlarge + 511) / 512;
 		p.info->num_binning_dispatches[0] = uint32_t(min(max(tasks, 4), kMaxDispatches));
@@ -166,9 +168,12 @@ __global__ void __launch_bounds__(kBinningThreads, 1) binCountKernel(FrameParams
 
 // ---------------------------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(1024) binCategorizeKernel(FrameParams p) {
+template <class Src> __global__ void __launch_bounds__(1024) binCategorizeKernel(Src src) {
 	__shared__ uint32_t s_scan[33];
 	__shared__ int s_iscan[33];
+	__shared__ uint32_t s_base[2];
+	int cta, ncta;
+	const FrameParams& p = src.get(cta, ncta);
 	const int bins = p.bin_count;
 	const int per = (bins + blockDim.x - 1) / blockDim.x;
 	const int beg = min(bins, int(threadIdx.x) * per), end = min(bins, beg + per);
@@ -190,6 +195,14 @@ __global__ void __launch_bounds__(1024) binCategorizeKernel(FrameParams p) {
 	uint32_t tq, tt;
 	uint32_t oq = blockExclusiveScan(lq, s_scan, &tq);
 	uint32_t ot = blockExclusiveScan(lt, s_scan, &tt);
+	// views of a batch take their lists from the shared reference buffers
+	if(threadIdx.x == 0) {
+		s_base[0] = p.ref_alloc ? atomicAdd(&p.ref_alloc[0], tq) : 0u;
+		s_base[1] = p.ref_alloc ? atomicAdd(&p.ref_alloc[1], tt) : 0u;
+	}
+	__syncthreads();
+	const uint32_t base_q = s_base[0], base_t = s_base[1];
+	oq += base_q, ot += base_t;
 	int tlow, thigh, tempty;
 	int olow = blockExclusiveScan(nlow, s_iscan, &tlow);
 	int ohigh = blockExclusiveScan(nhigh, s_iscan, &thigh);
@@ -230,20 +243,22 @@ __global__ void __launch_bounds__(1024) binCategorizeKernel(FrameParams p) {
 	if(threadIdx.x == 0) {
 		p.info->num_bin_quad_refs = tq;
 		p.info->num_bin_tri_refs = tt;
-		if(tq > uint32_t(p.max_bin_refs) || tt > uint32_t(p.max_bin_refs))
-			raiseError(p.info, LUCID_ERR_BIN_REFS, tq, tt, uint32_t(p.max_bin_refs));
+		if(uint64_t(base_q) + tq > uint64_t(p.max_bin_refs) || uint64_t(base_t) + tt > uint64_t(p.max_bin_refs))
+			raiseError(p.info, LUCID_ERR_BIN_REFS, base_q + tq, base_t + tt, uint32_t(p.max_bin_refs));
 	}
 }
 
 // ---------------------------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(kBinningThreads, 1) binDispatchKernel(FrameParams p) {
+template <class Src> __global__ void __launch_bounds__(kBinningThreads, 1) binDispatchKernel(Src src) {
 	extern __shared__ int s_bins[];
+	int cta, ncta;
+	const FrameParams& p = src.get(cta, ncta);
 	const int bins = p.bin_count, bcx = p.bin_count_x;
 	const int mvq = p.max_visible_quads;
 	const uint32_t cap = uint32_t(p.max_bin_refs);
 	const int nsmall = p.info->num_visible_quads[0], nlarge = p.info->num_visible_quads[1];
-	const int* hist = p.bin_batches + size_t(blockIdx.x) * 2 * bins;
+	const int* hist = p.bin_batches + size_t(cta) * 2 * bins;
 
 	// ---- small quads (bin_dispatcher.glsl:66-80, 202-232)
 	for(int i = threadIdx.x; i < bins; i += blockDim.x) {
@@ -252,7 +267,7 @@ __global__ void __launch_bounds__(kBinningThreads, 1) binDispatchKernel(FramePar
 	}
 	__syncthreads();
 	int sbeg, send;
-	ctaRange(nsmall, sbeg, send);
+	ctaRange(nsmall, cta, ncta, sbeg, send);
 	for(int k = sbeg + threadIdx.x; k < send; k += blockDim.x) {
 		uint32_t enc = p.quad_aabbs[k];
 		uint32_t entry = uint32_t(k) | (enc & 0xf0000000u);
@@ -274,7 +289,7 @@ __global__ void __launch_bounds__(kBinningThreads, 1) binDispatchKernel(FramePar
 	}
 	__syncthreads();
 	int lbeg, lend;
-	ctaRange(nlarge, lbeg, lend);
+	ctaRange(nlarge, cta, ncta, lbeg, lend);
 	int items = 2 * (lend - lbeg);
 	for(int it = threadIdx.x; it < items; it += blockDim.x) {
 		int k = lbeg + (it >> 1), second = it & 1;
@@ -304,13 +319,22 @@ __global__ void __launch_bounds__(kBinningThreads, 1) binDispatchKernel(FramePar
 // ---------------------------------------------------------------------------------------------
 
 void launchBinCount(const FrameParams& p, cudaStream_t stream) {
-	binCountKernel<<<p.num_binning_ctas, kBinningThreads, p.bin_count * sizeof(int), stream>>>(p);
+	binCountKernel<<<p.num_binning_ctas, kBinningThreads, p.bin_count * sizeof(int), stream>>>(OneView{p});
 }
 void launchBinCategorize(const FrameParams& p, cudaStream_t stream) {
-	binCategorizeKernel<<<1, 1024, 0, stream>>>(p);
+	binCategorizeKernel<<<1, 1024, 0, stream>>>(OneView{p});
 }
 void launchBinDispatch(const FrameParams& p, cudaStream_t stream) {
-	binDispatchKernel<<<p.num_binning_ctas, kBinningThreads, p.bin_count * sizeof(int), stream>>>(p);
+	binDispatchKernel<<<p.num_binning_ctas, kBinningThreads, p.bin_count * sizeof(int), stream>>>(OneView{p});
+}
+
+void launchBinningBatch(const BatchViews& per_view, const BatchViews& binning_ctas, int max_bins,
+						cudaStream_t stream) {
+	const int n = binning_ctas.cta_off[binning_ctas.num_views];
+	const size_t smem = size_t(max_bins) * sizeof(int);
+	binCountKernel<<<n, kBinningThreads, smem, stream>>>(binning_ctas);
+	binCategorizeKernel<<<per_view.num_views, 1024, 0, stream>>>(per_view);
+	binDispatchKernel<<<n, kBinningThreads, smem, stream>>>(binning_ctas);
 }
 
 } // namespace lucid

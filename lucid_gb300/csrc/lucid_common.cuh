@@ -77,12 +77,65 @@ struct FrameParams {
 	const float* dl_dimage;
 	float* dvertex_rgba;
 	float* dtri_opacity;
+	// batched frames: shared bump allocator of the bin reference lists (null for one view,
+	// whose lists start at 0)
+	uint32_t* ref_alloc; // [0] quad refs, [1] tri refs
+	// fragment store of the differentiable forward (kRasterStore): every pixel's fragments as
+	// tri slots in blend order
+	uint32_t* grad_tris;
+	uint32_t* grad_px_off;              // per pixel: first stored fragment
+	uint32_t* grad_px_cnt;              // per pixel: stored fragments
+	unsigned long long* grad_state;     // [0] overflow flag, [1] fragments allocated
+	unsigned long long grad_capacity;   // fragments grad_tris holds
 };
+
+// ---------------------------------------------------------------------------------------------
+// View sources of the pass kernels. A kernel is instantiated for one view (its FrameParams in
+// the parameter bank) or for a batch of views (FrameParams in device memory; each CTA range
+// belongs to one view, whose parameters the CTA copies to shared memory).
+
+constexpr int kMaxBatchViews = 256;
+
+struct OneView {
+	FrameParams p;
+	__device__ __forceinline__ const FrameParams& get(int& cta, int& ncta) const {
+		cta = blockIdx.x, ncta = gridDim.x;
+		return p;
+	}
+};
+
+struct BatchViews {
+	const FrameParams* views;
+	int num_views;
+	int cta_off[kMaxBatchViews + 1]; // CTAs [cta_off[v], cta_off[v + 1]) work on view v
+
+	__device__ __forceinline__ const FrameParams& get(int& cta, int& ncta) const {
+		__shared__ __align__(16) FrameParams s_view;
+		const int c = int(blockIdx.x);
+		int lo = 0, hi = num_views - 1;
+		while(lo < hi) { // last view whose range starts at or before c (skips empty ranges)
+			int mid = (lo + hi + 1) >> 1;
+			if(cta_off[mid] <= c)
+				lo = mid;
+			else
+				hi = mid - 1;
+		}
+		cta = c - cta_off[lo], ncta = cta_off[lo + 1] - cta_off[lo];
+		const uint32_t* src = reinterpret_cast<const uint32_t*>(views + lo);
+		uint32_t* dst = reinterpret_cast<uint32_t*>(&s_view);
+		for(int i = threadIdx.x; i < int(sizeof(FrameParams) / 4); i += blockDim.x)
+			dst[i] = src[i];
+		__syncthreads();
+		return s_view;
+	}
+};
+static_assert(sizeof(FrameParams) % 4 == 0, "FrameParams is copied as 32-bit words");
 
 // Raster kernel modes.
 constexpr int kRasterForward = 0;  // image
 constexpr int kRasterStats = 1;    // image + per-pixel FP64 colour for the backward pass
 constexpr int kRasterBackward = 2; // gradients of vertex RGBA / triangle opacity
+constexpr int kRasterStore = 3;    // each pixel's sorted fragments into the fragment store
 
 // Offsets into the per-bin counter array (definitions.glsl:117-129)
 __device__ __forceinline__ uint32_t& binQuadCounts(const FrameParams& p, int i) { return p.counts[p.bin_count * 0 + i]; }

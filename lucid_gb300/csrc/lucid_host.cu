@@ -96,11 +96,21 @@ struct lucid_renderer {
 	double* px_color64 = nullptr;
 	float* px_color32 = nullptr;
 	float* stats_image = nullptr;
+	uint32_t* grad_px_off = nullptr;
+	uint32_t* grad_px_cnt = nullptr;
+	unsigned long long* grad_state = nullptr;  // [0] store overflow, [1] fragments of the last frame
+	uint32_t* grad_tris = nullptr;             // fragment store (own allocation, grows)
+	size_t grad_capacity = 0;
+	unsigned long long* grad_need_host = nullptr; // pinned copy of grad_state[1]
+	cudaEvent_t grad_need_event = nullptr;
+	bool grad_need_pending = false;
 	// set by lucid_render_forward_grad, cleared by every other pass: the bin lists and the
 	// per-pixel colours then belong to grad_inputs / grad_config
 	bool grad_ready = false;
 	lucid_frame_inputs grad_inputs{};
 	lucid_config grad_config{};
+
+	struct BatchPlan* batch = nullptr; // lucid_render_batch state (plan, buffers, graph)
 
 	size_t infoBytes() const { return sizeof(lucid_info) + size_t(10) * bin_count * 4; }
 	lucid_info* info() const { return reinterpret_cast<lucid_info*>(info_block); }
@@ -443,9 +453,20 @@ extern "C" lucid_status lucid_create(const lucid_options* options, int32_t width
 	return LUCID_OK;
 }
 
+static void destroyBatchPlan(lucid_renderer* r);
+
 extern "C" lucid_status lucid_destroy(lucid_renderer* r) {
 	if(!r)
 		return LUCID_OK;
+	destroyBatchPlan(r);
+	if(r->grad_need_event)
+		cudaEventSynchronize(r->grad_need_event);
+	if(r->grad_tris)
+		cudaFree(r->grad_tris);
+	if(r->grad_need_host)
+		cudaFreeHost(r->grad_need_host);
+	if(r->grad_need_event)
+		cudaEventDestroy(r->grad_need_event);
 	freeAll(r);
 	delete r;
 	return LUCID_OK;
@@ -635,28 +656,111 @@ lucid_status checkGradInputs(lucid_renderer* r, const lucid_frame_inputs* in) {
 		const size_t npix = size_t(r->width) * r->height;
 		if((st = allocate(r, &r->px_color64, npix * 3)) != LUCID_OK ||
 		   (st = allocate(r, &r->px_color32, npix * 3)) != LUCID_OK ||
-		   (st = allocate(r, &r->stats_image, npix * 4)) != LUCID_OK)
+		   (st = allocate(r, &r->stats_image, npix * 4)) != LUCID_OK ||
+		   (st = allocate(r, &r->grad_px_off, npix)) != LUCID_OK ||
+		   (st = allocate(r, &r->grad_px_cnt, npix)) != LUCID_OK ||
+		   (st = allocate(r, &r->grad_state, 2)) != LUCID_OK)
 			return st;
+		cudaError_t err = cudaHostAlloc(reinterpret_cast<void**>(&r->grad_need_host), 8, cudaHostAllocDefault);
+		if(err == cudaSuccess)
+			err = cudaEventCreateWithFlags(&r->grad_need_event, cudaEventDisableTiming);
+		if(err != cudaSuccess)
+			return cudaFail(err, "gradient pass host state");
 	}
 	return LUCID_OK;
 }
 
-// setup, binning and the stats raster pass (image + per-pixel FP64 colour)
+// Sizes the fragment store: a fixed capacity, none, or (automatic) at least 2^25 fragments and
+// 1.25x the fragments of the last differentiable frame once that count is known on the host.
+lucid_status ensureGradStore(lucid_renderer* r, cudaStream_t s) {
+	const int32_t opt = r->opts.grad_store_fragments;
+	size_t want = r->grad_capacity;
+	if(opt > 0) {
+		want = size_t(opt);
+	} else if(opt == 0) {
+		want = std::max(want, size_t(1) << 25);
+		if(r->grad_need_pending && cudaEventQuery(r->grad_need_event) == cudaSuccess) {
+			r->grad_need_pending = false;
+			const unsigned long long need = *r->grad_need_host;
+			if(need > r->grad_capacity)
+				want = std::max(want, size_t(need + need / 4));
+		}
+		cudaGetLastError(); // cudaEventQuery's cudaErrorNotReady
+		want = std::min(want, size_t(0xffffffffu));
+	} else {
+		want = 0;
+	}
+	if(want == r->grad_capacity)
+		return LUCID_OK;
+	LUCID_CUDA_TRY(cudaStreamSynchronize(s));
+	if(r->grad_tris) {
+		cudaFree(r->grad_tris);
+		r->grad_tris = nullptr;
+		r->grad_capacity = 0;
+	}
+	if(want > 0) {
+		cudaError_t err = cudaMalloc(&r->grad_tris, want * sizeof(uint32_t));
+		if(err != cudaSuccess) {
+			cudaGetLastError();
+			r->grad_tris = nullptr; // no store: the backward pass recomputes the fragment lists
+			return LUCID_OK;
+		}
+		r->grad_capacity = want;
+	}
+	return LUCID_OK;
+}
+
+FrameParams gradParams(lucid_renderer* r) {
+	FrameParams p = r->last;
+	p.px_color64 = r->px_color64;
+	p.px_color32 = r->px_color32;
+	p.grad_tris = r->grad_tris;
+	p.grad_px_off = r->grad_px_off;
+	p.grad_px_cnt = r->grad_px_cnt;
+	p.grad_state = r->grad_state;
+	p.grad_capacity = r->grad_capacity;
+	return p;
+}
+
+// Setup, binning and the differentiable forward: the raster pass in store mode and the
+// pixel-parallel FP64 colour kernel, or, when the store cannot hold the frame, the raster
+// pass's FP64 colour mode. Both alternatives are launched; each checks the store's overflow
+// flag on the device and returns at once when it is not the one needed, so the host never
+// waits for the outcome.
 lucid_status gradForward(lucid_renderer* r, const lucid_frame_inputs* in, float* out, void* stream) {
 	lucid_status st;
+	cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+	if((st = ensureGradStore(r, s)) != LUCID_OK)
+		return st;
 	if((st = lucid_quad_setup(r, in, stream)) != LUCID_OK || (st = lucid_bin_count(r, stream)) != LUCID_OK ||
 	   (st = lucid_bin_categorize(r, stream)) != LUCID_OK || (st = lucid_bin_dispatch(r, stream)) != LUCID_OK)
 		return st;
-	cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-	FrameParams p = r->last;
+	FrameParams p = gradParams(r);
 	p.out_rgba = out;
-	p.px_color64 = r->px_color64;
-	p.px_color32 = r->px_color32;
+	const size_t npix = size_t(r->width) * r->height;
+	LUCID_CUDA_TRY(cudaMemsetAsync(r->grad_state, 0, 16, s));
+	if(r->grad_capacity == 0)
+		LUCID_CUDA_TRY(cudaMemsetAsync(r->grad_state, 1, 8, s)); // no store: flag it full
+	LUCID_CUDA_TRY(cudaMemsetAsync(r->grad_px_cnt, 0, npix * 4, s));
 	if((st = resetRasterCounters(r, s)) != LUCID_OK)
 		return st;
+	if(r->grad_capacity > 0) {
+		launchRaster(p, r->raster_ctas, s, kRasterStore);
+		if((st = checkLaunch("raster (store)")) != LUCID_OK)
+			return st;
+	}
+	LUCID_CUDA_TRY(cudaMemsetAsync(&r->info()->raster_work_counter, 0, 4, s));
 	launchRaster(p, r->raster_ctas, s, kRasterStats);
-	if((st = checkLaunch("raster (stats)")) != LUCID_OK)
+	if((st = checkLaunch("raster (FP64 colour)")) != LUCID_OK)
 		return st;
+	launchGradColor(p, s);
+	if((st = checkLaunch("gradient colour")) != LUCID_OK)
+		return st;
+	if(r->grad_capacity > 0 && r->opts.grad_store_fragments == 0) {
+		LUCID_CUDA_TRY(cudaMemcpyAsync(r->grad_need_host, &r->grad_state[1], 8, cudaMemcpyDeviceToHost, s));
+		LUCID_CUDA_TRY(cudaEventRecord(r->grad_need_event, s));
+		r->grad_need_pending = true;
+	}
 	r->grad_ready = true;
 	r->grad_inputs = *in;
 	r->grad_config = *in->config;
@@ -685,6 +789,8 @@ extern "C" lucid_status lucid_render_backward(lucid_renderer* r, const lucid_fra
 		return st;
 	if(dvertex_rgba && in->color_format != LUCID_COLOR_RGBA32F)
 		return fail(LUCID_INVALID_ARG, "vertex colour gradients need LUCID_COLOR_RGBA32F colours");
+	if(reinterpret_cast<uintptr_t>(dvertex_rgba) % 16 != 0)
+		return fail(LUCID_INVALID_ARG, "dvertex_rgba must be 16-byte aligned");
 	if(dtri_opacity && !in->tri_opacity)
 		return fail(LUCID_INVALID_ARG, "opacity gradients need inputs->tri_opacity");
 	// Reuse the forward pass's bin lists and per-pixel colours when the last pass on this
@@ -695,24 +801,321 @@ extern "C" lucid_status lucid_render_backward(lucid_renderer* r, const lucid_fra
 					   memcmp(&r->grad_config, in->config, sizeof(lucid_config)) == 0;
 	if(!reuse && (st = gradForward(r, in, r->stats_image, stream)) != LUCID_OK)
 		return st;
+	// the pixel-parallel backward over the fragment store, or (store overflowed) the raster
+	// pass's backward mode; each returns at once when it is not the one needed
 	cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-	FrameParams p = r->last;
+	FrameParams p = gradParams(r);
 	p.out_rgba = r->stats_image;
-	p.px_color64 = r->px_color64;
-	p.px_color32 = r->px_color32;
 	p.dl_dimage = dl_dimage;
 	p.dvertex_rgba = dvertex_rgba;
 	p.dtri_opacity = dtri_opacity;
-	if((st = resetRasterCounters(r, s)) != LUCID_OK)
+	launchGradBackward(p, s);
+	if((st = checkLaunch("gradient backward")) != LUCID_OK)
 		return st;
+	LUCID_CUDA_TRY(cudaMemsetAsync(&r->info()->raster_work_counter, 0, 4, s));
 	launchRaster(p, r->raster_ctas, s, kRasterBackward);
 	return checkLaunch("raster (backward)");
 }
 
+// ---------------------------------------------------------------------------------------------
+// Batched frames (no reference counterpart)
+//
+// A batch renders every view with one launch per pass: CTA ranges of the setup and binning
+// kernels map to views, and one persistent raster kernel walks the (view, bin) work list of all
+// views. Views take consecutive slices of the renderer's quad / tri record buffers (capacity =
+// the view's input quads) and share the bin reference lists through a device bump allocator.
+// The launch sequence of a batch topology (view count, sizes, quad and instance counts) is
+// recorded once as a CUDA graph and replayed by later calls; the graph's first node copies the
+// views' parameters (input pointers, configs) from a pinned staging block, rewritten only when
+// they change.
+
+struct BatchPlan {
+	std::vector<int64_t> key;
+	int num_views = 0;
+	int max_bins = 0;
+	std::vector<FrameParams> params; // what params_pinned holds
+	std::vector<size_t> info_off;    // byte offset of each view's info block in `infos`
+	size_t info_bytes = 0;
+	BatchViews per_view{}, setup_map{}, binning_map{};
+	std::vector<void*> allocations;
+	FrameParams* params_dev = nullptr;
+	FrameParams* params_pinned = nullptr;
+	unsigned char* infos = nullptr;
+	int* inst_offsets = nullptr;
+	int4* setup_counts = nullptr;
+	int4* setup_offsets = nullptr;
+	int* bin_batches = nullptr;
+	uint32_t* raster_work = nullptr;
+	int* level_prefix = nullptr;
+	uint32_t* counters = nullptr; // [0] quad refs, [1] tri refs, [2] raster work
+	cudaStream_t capture_stream = nullptr;
+	cudaEvent_t done = nullptr;
+	cudaGraphExec_t exec = nullptr;
+};
+
+static void destroyBatchPlan(lucid_renderer* r) {
+	BatchPlan* b = r->batch;
+	if(!b)
+		return;
+	if(b->done)
+		cudaEventSynchronize(b->done);
+	if(b->exec)
+		cudaGraphExecDestroy(b->exec);
+	if(b->done)
+		cudaEventDestroy(b->done);
+	if(b->capture_stream)
+		cudaStreamDestroy(b->capture_stream);
+	if(b->params_pinned)
+		cudaFreeHost(b->params_pinned);
+	for(void* p : b->allocations)
+		cudaFree(p);
+	delete b;
+	r->batch = nullptr;
+}
+
+namespace {
+
+template <typename T> lucid_status batchAlloc(BatchPlan* b, T** ptr, size_t count) {
+	void* p = nullptr;
+	size_t bytes = std::max<size_t>(count * sizeof(T), 16);
+	cudaError_t err = cudaMalloc(&p, bytes);
+	if(err != cudaSuccess) {
+		cudaGetLastError();
+		return fail(LUCID_OUT_OF_MEMORY, std::string("batch cudaMalloc(") + std::to_string(bytes) +
+											 " bytes): " + cudaGetErrorString(err));
+	}
+	b->allocations.push_back(p);
+	*ptr = reinterpret_cast<T*>(p);
+	return LUCID_OK;
+}
+
+int viewBins(int w, int h) { return ((w + kBinSize - 1) / kBinSize) * ((h + kBinSize - 1) / kBinSize); }
+int viewSetupCtas(int nq) { return (nq + kSetupThreads - 1) / kSetupThreads; }
+int viewBinningCtas(const lucid_renderer* r, int nq) {
+	return std::max(1, std::min(r->opts.binning_ctas, (nq + 2047) / 2048));
+}
+
+std::vector<int64_t> batchKey(const lucid_view* views, int n) {
+	std::vector<int64_t> key;
+	key.reserve(1 + 4 * size_t(n));
+	key.push_back(n);
+	for(int v = 0; v < n; v++) {
+		key.push_back(views[v].width);
+		key.push_back(views[v].height);
+		key.push_back(views[v].inputs.num_quads);
+		key.push_back(views[v].inputs.num_instances);
+	}
+	return key;
+}
+
+// Parameters of every view, pointing into the plan's and the renderer's buffers.
+void batchParams(lucid_renderer* r, BatchPlan* b, const lucid_view* views, std::vector<FrameParams>& out) {
+	const int n = b->num_views;
+	out.assign(size_t(n), FrameParams{});
+	size_t qbase = 0, ibase = 0, sbase = 0, bbase = 0, rbase = 0;
+	for(int v = 0; v < n; v++) {
+		const lucid_view& vw = views[v];
+		const lucid_frame_inputs& in = vw.inputs;
+		FrameParams& p = out[size_t(v)];
+		p.positions = in.positions;
+		p.colors = in.colors;
+		p.color_format = in.color_format;
+		p.num_verts = in.num_verts;
+		p.quads_ib = in.quads_ib;
+		p.num_quads = in.num_quads;
+		p.num_instances = in.num_instances;
+		p.instances = in.instances;
+		p.instance_colors = in.instance_colors;
+		p.tri_opacity = in.tri_opacity;
+		p.out_rgba = vw.out_rgba;
+		p.cfg = *in.config;
+		p.width = vw.width, p.height = vw.height;
+		p.bin_count_x = (vw.width + kBinSize - 1) / kBinSize;
+		p.bin_count_y = (vw.height + kBinSize - 1) / kBinSize;
+		p.bin_count = p.bin_count_x * p.bin_count_y;
+		const int nq = in.num_quads;
+		const int cap = std::max(nq, 1);
+		p.max_visible_quads = cap;
+		p.max_bin_refs = r->opts.max_bin_refs;
+		p.band_capacity = r->opts.band_capacity;
+		p.low_high_threshold = r->opts.low_high_threshold;
+		p.num_setup_ctas = viewSetupCtas(nq);
+		p.num_binning_ctas = viewBinningCtas(r, nq);
+		p.flags = r->opts.flags & ~uint32_t(LUCID_OPT_TIMERS);
+		p.info = reinterpret_cast<lucid_info*>(b->infos + b->info_off[size_t(v)]);
+		p.counts = reinterpret_cast<uint32_t*>(b->infos + b->info_off[size_t(v)] + sizeof(lucid_info));
+		p.inst_offsets = b->inst_offsets + ibase;
+		p.quad_class = r->quad_class + qbase;
+		p.setup_cta_counts = b->setup_counts + sbase;
+		p.setup_cta_offsets = b->setup_offsets + sbase;
+		p.quad_aabbs = r->quad_aabbs + qbase;
+		p.quad_source = r->quad_source + qbase;
+		p.quad_verts = r->quad_verts + qbase;
+		p.quad_colors = r->quad_colors + qbase;
+		p.tri_bary = r->tri_bary + 4 * qbase;
+		p.tri_scan = r->tri_scan + 4 * qbase;
+		p.tri_depth = r->tri_depth + 2 * qbase;
+		p.tri_normals = r->tri_normals + 2 * qbase;
+		p.bin_quads = r->bin_quads;
+		p.bin_tris = r->bin_tris;
+		p.bin_batches = b->bin_batches + bbase;
+		p.raster_work = b->raster_work + rbase;
+		p.band_scratch = r->band_scratch;
+		p.ref_alloc = b->counters;
+		qbase += size_t(cap);
+		ibase += size_t(in.num_instances) + 1;
+		sbase += size_t(std::max(p.num_setup_ctas, 1));
+		bbase += size_t(p.num_binning_ctas) * 2 * size_t(p.bin_count);
+		rbase += size_t(p.bin_count);
+	}
+}
+
+lucid_status buildBatchPlan(lucid_renderer* r, const lucid_view* views, int n, std::vector<int64_t> key,
+							cudaStream_t user_stream) {
+	// the previous plan's graph may still run on the caller's stream
+	LUCID_CUDA_TRY(cudaStreamSynchronize(user_stream));
+	destroyBatchPlan(r);
+	BatchPlan* b = new BatchPlan();
+	r->batch = b;
+	b->key = std::move(key);
+	b->num_views = n;
+	size_t quads = 0, insts = 0, setup_ctas = 0, hist = 0, bins = 0;
+	b->info_off.resize(size_t(n));
+	for(int v = 0; v < n; v++) {
+		const int nq = views[v].inputs.num_quads;
+		const int vb = viewBins(views[v].width, views[v].height);
+		b->max_bins = std::max(b->max_bins, vb);
+		quads += size_t(std::max(nq, 1));
+		insts += size_t(views[v].inputs.num_instances) + 1;
+		setup_ctas += size_t(std::max(viewSetupCtas(nq), 1));
+		hist += size_t(viewBinningCtas(r, nq)) * 2 * size_t(vb);
+		bins += size_t(vb);
+		b->info_off[size_t(v)] = b->info_bytes;
+		b->info_bytes += (sizeof(lucid_info) + size_t(10) * vb * 4 + 255) & ~size_t(255);
+	}
+	lucid_status st;
+	if(quads > size_t(r->opts.max_visible_quads) || quads > size_t(r->opts.max_input_quads)) {
+		destroyBatchPlan(r);
+		return fail(LUCID_CAPACITY_EXCEEDED, "batch: total quads " + std::to_string(quads) +
+												  " exceed options.max_visible_quads / max_input_quads");
+	}
+	auto bail = [&](lucid_status e) {
+		destroyBatchPlan(r);
+		return e;
+	};
+	if((st = batchAlloc(b, &b->params_dev, size_t(n))) != LUCID_OK ||
+	   (st = batchAlloc(b, &b->infos, b->info_bytes)) != LUCID_OK ||
+	   (st = batchAlloc(b, &b->inst_offsets, insts)) != LUCID_OK ||
+	   (st = batchAlloc(b, &b->setup_counts, setup_ctas)) != LUCID_OK ||
+	   (st = batchAlloc(b, &b->setup_offsets, setup_ctas)) != LUCID_OK ||
+	   (st = batchAlloc(b, &b->bin_batches, hist)) != LUCID_OK ||
+	   (st = batchAlloc(b, &b->raster_work, bins)) != LUCID_OK ||
+	   (st = batchAlloc(b, &b->level_prefix, size_t(3) * (n + 1))) != LUCID_OK ||
+	   (st = batchAlloc(b, &b->counters, 4)) != LUCID_OK)
+		return bail(st);
+	cudaError_t err = cudaHostAlloc(reinterpret_cast<void**>(&b->params_pinned), sizeof(FrameParams) * size_t(n),
+									cudaHostAllocDefault);
+	if(err != cudaSuccess)
+		return bail(cudaFail(err, "cudaHostAlloc (batch parameters)"));
+	if((err = cudaStreamCreateWithFlags(&b->capture_stream, cudaStreamNonBlocking)) != cudaSuccess ||
+	   (err = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming)) != cudaSuccess)
+		return bail(cudaFail(err, "batch stream / event"));
+
+	// CTA maps of the passes
+	BatchViews* maps[3] = {&b->per_view, &b->setup_map, &b->binning_map};
+	for(BatchViews* m : maps) {
+		m->views = b->params_dev;
+		m->num_views = n;
+		m->cta_off[0] = 0;
+	}
+	for(int v = 0; v < n; v++) {
+		const int nq = views[v].inputs.num_quads;
+		b->per_view.cta_off[v + 1] = v + 1;
+		b->setup_map.cta_off[v + 1] = b->setup_map.cta_off[v] + viewSetupCtas(nq);
+		b->binning_map.cta_off[v + 1] = b->binning_map.cta_off[v] + viewBinningCtas(r, nq);
+	}
+
+	// record the frame
+	cudaStream_t cs = b->capture_stream;
+	if((err = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+		return bail(cudaFail(err, "cudaStreamBeginCapture"));
+	cudaMemcpyAsync(b->params_dev, b->params_pinned, sizeof(FrameParams) * size_t(n), cudaMemcpyHostToDevice, cs);
+	cudaMemsetAsync(b->infos, 0, b->info_bytes, cs);
+	cudaMemsetAsync(b->counters, 0, 16, cs);
+	launchSetupBatch(b->per_view, b->setup_map, cs);
+	launchBinningBatch(b->per_view, b->binning_map, b->max_bins, cs);
+	launchRasterBatch(b->params_dev, n, b->level_prefix, b->counters + 2, r->raster_ctas, cs);
+	cudaGraph_t graph = nullptr;
+	cudaError_t cap_err = cudaStreamEndCapture(cs, &graph);
+	cudaError_t launch_err = cudaGetLastError();
+	if(cap_err != cudaSuccess || launch_err != cudaSuccess) {
+		if(graph)
+			cudaGraphDestroy(graph);
+		return bail(cudaFail(cap_err != cudaSuccess ? cap_err : launch_err, "batch capture"));
+	}
+	err = cudaGraphInstantiate(&b->exec, graph, 0);
+	cudaGraphDestroy(graph);
+	if(err != cudaSuccess)
+		return bail(cudaFail(err, "cudaGraphInstantiate"));
+	return LUCID_OK;
+}
+
+} // namespace
+
 extern "C" lucid_status lucid_render_batch(lucid_renderer* r, const lucid_view* views,
 										   int32_t num_views, void* stream) {
-	(void)r, (void)views, (void)num_views, (void)stream;
-	return fail(LUCID_NOT_SUPPORTED, "lucid_render_batch is not built yet");
+	if(!r || !views || num_views <= 0)
+		return fail(LUCID_INVALID_ARG, "lucid_render_batch: renderer, views and num_views > 0 are required");
+	if(num_views > r->opts.max_views || num_views > kMaxBatchViews)
+		return fail(LUCID_CAPACITY_EXCEEDED, "lucid_render_batch: num_views " + std::to_string(num_views) +
+												  " > options.max_views (at most " + std::to_string(kMaxBatchViews) +
+												  ")");
+	for(int v = 0; v < num_views; v++) {
+		const lucid_view& vw = views[v];
+		if(vw.width <= 0 || vw.height <= 0 || vw.width > r->width || vw.height > r->height)
+			return fail(LUCID_INVALID_ARG, "view " + std::to_string(v) + ": size must be within the renderer's");
+		if(!vw.out_rgba)
+			return fail(LUCID_INVALID_ARG, "view " + std::to_string(v) + ": out_rgba is NULL");
+		lucid_status st = validateInputs(r, &vw.inputs);
+		if(st != LUCID_OK)
+			return fail(st, "view " + std::to_string(v) + ": " + g_last_error);
+	}
+	cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+	cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+	LUCID_CUDA_TRY(cudaStreamIsCapturing(s, &cap));
+	if(cap != cudaStreamCaptureStatusNone)
+		return fail(LUCID_NOT_SUPPORTED, "lucid_render_batch records and replays its own CUDA graph; "
+										 "call it outside stream capture");
+	r->have_frame = false; // the single-view buffers are reused by the batch
+	r->grad_ready = false;
+	std::vector<int64_t> key = batchKey(views, num_views);
+	lucid_status st;
+	if(!r->batch || r->batch->key != key) {
+		if((st = buildBatchPlan(r, views, num_views, std::move(key), s)) != LUCID_OK)
+			return st;
+	}
+	BatchPlan* b = r->batch;
+	std::vector<FrameParams> params;
+	batchParams(r, b, views, params);
+	const size_t bytes = sizeof(FrameParams) * params.size();
+	if(b->params.size() != params.size() || memcmp(b->params.data(), params.data(), bytes) != 0) {
+		// the previous replay's copy node must have read the staging block first
+		LUCID_CUDA_TRY(cudaEventSynchronize(b->done));
+		memcpy(b->params_pinned, params.data(), bytes);
+		b->params.swap(params);
+	}
+	LUCID_CUDA_TRY(cudaGraphLaunch(b->exec, s));
+	LUCID_CUDA_TRY(cudaEventRecord(b->done, s));
+	return LUCID_OK;
+}
+
+extern "C" lucid_status lucid_get_batch_info(lucid_renderer* r, int32_t view, lucid_info* out, void* stream) {
+	if(!r || !out || !r->batch || view < 0 || view >= r->batch->num_views)
+		return fail(LUCID_INVALID_ARG, "lucid_get_batch_info: no such view of the last batch");
+	LUCID_CUDA_TRY(cudaStreamSynchronize(reinterpret_cast<cudaStream_t>(stream)));
+	LUCID_CUDA_TRY(cudaMemcpy(out, r->batch->infos + r->batch->info_off[size_t(view)], sizeof(lucid_info),
+							  cudaMemcpyDeviceToHost));
+	return LUCID_OK;
 }
 
 extern "C" lucid_status lucid_autotune(lucid_renderer* r, const lucid_frame_inputs* in,

@@ -10,6 +10,15 @@ void launchBinCount(const FrameParams& p, cudaStream_t stream);
 void launchBinCategorize(const FrameParams& p, cudaStream_t stream);
 void launchBinDispatch(const FrameParams& p, cudaStream_t stream);
 void launchRaster(const FrameParams& p, int num_ctas, cudaStream_t stream, int mode = kRasterForward);
+// Batched frames: one launch per pass for every view (CTA ranges per view in the maps).
+void launchSetupBatch(const BatchViews& per_view, const BatchViews& setup_ctas, cudaStream_t stream);
+void launchBinningBatch(const BatchViews& per_view, const BatchViews& binning_ctas, int max_bins,
+						cudaStream_t stream);
+void launchRasterBatch(const FrameParams* views_dev, int num_views, int* level_prefix, uint32_t* counter,
+					   int num_ctas, cudaStream_t stream);
+// Differentiable frames: pixel-parallel kernels over the fragment store.
+void launchGradColor(const FrameParams& p, cudaStream_t stream);
+void launchGradBackward(const FrameParams& p, cudaStream_t stream);
 size_t rasterSmemBytes();
 int rasterThreads();
 

@@ -30,6 +30,7 @@
 
 #include "lucid_common.cuh"
 #include "lucid_kernels.h"
+#include "lucid_shade.cuh"
 
 namespace lucid {
 
@@ -72,11 +73,16 @@ struct RasterSmem {
 	int scan_tmp[NW + 1];
 	uint32_t scan_tmpu[NW + 1];
 	unsigned long long stat_hbt;
+	unsigned long long store_base; // kRasterStore: first store slot of the bin
 	uint32_t kmin, kmax;
 	int bin;
 	int group_end;
 	int single_digit;
 	int any_big;
+	int view;        // view of the current bin (batched frames)
+	int loaded_view; // view whose parameters view_params holds
+	int store_ok;    // kRasterStore: the bin's fragments fit the store
+	FrameParams view_params;
 };
 
 static_assert(sizeof(RasterSmem) <= 227 * 1024, "raster shared memory exceeds one SM");
@@ -85,131 +91,6 @@ size_t rasterSmemBytes() { return sizeof(RasterSmem); }
 int rasterThreads() { return RT; }
 
 __device__ __forceinline__ uint32_t entryTri(uint2 e) { return (e.x >> 20) | ((e.y >> 20) << 12); }
-
-// Fragment colour (shading.glsl:107-165 without lighting/texturing; exact-mode FP32 colours).
-__device__ __forceinline__ float4 shadeFragment(const FrameParams& p, uint32_t tri, float inv_ray_pos,
-												int px, int py) {
-	uint4 b0r = __ldg(p.tri_bary + size_t(tri) * 2);
-	uint4 b1r = __ldg(p.tri_bary + size_t(tri) * 2 + 1);
-	uint32_t fid = __ldg(&p.tri_depth[tri].w);
-	float fx = float(px), fy = float(py);
-	float ray_pos = 1.0f / inv_ray_pos;
-	float e0 = bitsf(b0r.x) * fx + (bitsf(b0r.y) * fy + bitsf(b0r.z));
-	float e1 = bitsf(b1r.x) * fx + (bitsf(b1r.y) * fy + bitsf(b1r.z));
-	float b0 = e0 * ray_pos, b1 = e1 * ray_pos;
-	b0 = b0 - bitsf(b0r.w);
-	b1 = b1 - bitsf(b1r.w);
-	uint32_t flags = fid & 0xffffu, inst = fid >> 16;
-	float4 col = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
-	if((flags & LUCID_INST_HAS_COLOR) && p.instance_colors)
-		col = decodeRGBA8(__ldg(p.instance_colors + inst));
-	if(flags & LUCID_INST_HAS_VERTEX_COLORS) {
-		uint32_t quad = tri >> 1, second = tri & 1;
-		uint4 qv = __ldg(p.quad_verts + quad);
-		uint32_t v1 = second ? qv.z : qv.y, v2 = second ? qv.w : qv.z;
-		float4 c0, c1, c2;
-		if(p.color_format == LUCID_COLOR_RGBA8) {
-			uint4 qc = __ldg(p.quad_colors + quad);
-			c0 = decodeRGBA8(qc.x);
-			c1 = decodeRGBA8(second ? qc.z : qc.y);
-			c2 = decodeRGBA8(second ? qc.w : qc.z);
-		} else if(p.color_format == LUCID_COLOR_RGBA16F) {
-			const uint2* hc = reinterpret_cast<const uint2*>(p.colors);
-			uint2 h0 = __ldg(hc + qv.x), h1 = __ldg(hc + v1), h2 = __ldg(hc + v2);
-			auto cvt = [](uint2 h) {
-				__half2 a = *reinterpret_cast<__half2*>(&h.x), b = *reinterpret_cast<__half2*>(&h.y);
-				float2 fa = __half22float2(a), fb = __half22float2(b);
-				return make_float4(fa.x, fa.y, fb.x, fb.y);
-			};
-			c0 = cvt(h0), c1 = cvt(h1), c2 = cvt(h2);
-		} else {
-			const float4* fc = reinterpret_cast<const float4*>(p.colors);
-			c0 = __ldg(fc + qv.x), c1 = __ldg(fc + v1), c2 = __ldg(fc + v2);
-		}
-		float w = (1.0f - b0) - b1;
-		col.x = col.x * (w * c0.x + (b0 * c1.x + b1 * c2.x));
-		col.y = col.y * (w * c0.y + (b0 * c1.y + b1 * c2.y));
-		col.z = col.z * (w * c0.z + (b0 * c1.z + b1 * c2.z));
-		col.w = col.w * (w * c0.w + (b0 * c1.w + b1 * c2.w));
-	}
-	if(p.tri_opacity) {
-		uint32_t prim = __ldg(p.quad_source + (tri >> 1)) * 2 + (tri & 1);
-		col.w = col.w * __ldg(p.tri_opacity + prim);
-	}
-	return col;
-}
-
-// shadeFragment with everything the backward pass needs to route gradients to the vertex
-// colours and the triangle opacity (same float operations, so the same colour).
-struct FragmentShade {
-	float4 col;           // colour used by the blend (alpha includes the opacity)
-	float4 inst;          // instance colour factor
-	float wgt[3];         // barycentric weights of the three vertices
-	uint32_t vid[3];      // vertex ids
-	float opacity;        // per-triangle opacity factor (1 if none)
-	float alpha_pre;      // alpha before the opacity factor
-	uint32_t prim;
-	bool has_vc;
-};
-
-__device__ __forceinline__ FragmentShade shadeFragmentFull(const FrameParams& p, uint32_t tri,
-														   float inv_ray_pos, int px, int py) {
-	FragmentShade f;
-	uint4 b0r = __ldg(p.tri_bary + size_t(tri) * 2);
-	uint4 b1r = __ldg(p.tri_bary + size_t(tri) * 2 + 1);
-	uint32_t fid = __ldg(&p.tri_depth[tri].w);
-	float fx = float(px), fy = float(py);
-	float ray_pos = 1.0f / inv_ray_pos;
-	float e0 = bitsf(b0r.x) * fx + (bitsf(b0r.y) * fy + bitsf(b0r.z));
-	float e1 = bitsf(b1r.x) * fx + (bitsf(b1r.y) * fy + bitsf(b1r.z));
-	float b0 = e0 * ray_pos, b1 = e1 * ray_pos;
-	b0 = b0 - bitsf(b0r.w);
-	b1 = b1 - bitsf(b1r.w);
-	uint32_t flags = fid & 0xffffu, inst = fid >> 16;
-	f.inst = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
-	if((flags & LUCID_INST_HAS_COLOR) && p.instance_colors)
-		f.inst = decodeRGBA8(__ldg(p.instance_colors + inst));
-	f.col = f.inst;
-	float w = (1.0f - b0) - b1;
-	f.wgt[0] = w, f.wgt[1] = b0, f.wgt[2] = b1;
-	uint32_t quad = tri >> 1, second = tri & 1;
-	uint4 qv = __ldg(p.quad_verts + quad);
-	f.vid[0] = qv.x, f.vid[1] = second ? qv.z : qv.y, f.vid[2] = second ? qv.w : qv.z;
-	f.has_vc = (flags & LUCID_INST_HAS_VERTEX_COLORS) != 0;
-	if(f.has_vc) {
-		float4 c0, c1, c2;
-		if(p.color_format == LUCID_COLOR_RGBA8) {
-			uint4 qc = __ldg(p.quad_colors + quad);
-			c0 = decodeRGBA8(qc.x);
-			c1 = decodeRGBA8(second ? qc.z : qc.y);
-			c2 = decodeRGBA8(second ? qc.w : qc.z);
-		} else if(p.color_format == LUCID_COLOR_RGBA16F) {
-			const uint2* hc = reinterpret_cast<const uint2*>(p.colors);
-			uint2 h0 = __ldg(hc + f.vid[0]), h1 = __ldg(hc + f.vid[1]), h2 = __ldg(hc + f.vid[2]);
-			auto cvt = [](uint2 h) {
-				__half2 a = *reinterpret_cast<__half2*>(&h.x), b = *reinterpret_cast<__half2*>(&h.y);
-				float2 fa = __half22float2(a), fb = __half22float2(b);
-				return make_float4(fa.x, fa.y, fb.x, fb.y);
-			};
-			c0 = cvt(h0), c1 = cvt(h1), c2 = cvt(h2);
-		} else {
-			const float4* fc = reinterpret_cast<const float4*>(p.colors);
-			c0 = __ldg(fc + f.vid[0]), c1 = __ldg(fc + f.vid[1]), c2 = __ldg(fc + f.vid[2]);
-		}
-		f.col.x = f.col.x * (w * c0.x + (b0 * c1.x + b1 * c2.x));
-		f.col.y = f.col.y * (w * c0.y + (b0 * c1.y + b1 * c2.y));
-		f.col.z = f.col.z * (w * c0.z + (b0 * c1.z + b1 * c2.z));
-		f.col.w = f.col.w * (w * c0.w + (b0 * c1.w + b1 * c2.w));
-	}
-	f.alpha_pre = f.col.w;
-	f.opacity = 1.0f;
-	f.prim = __ldg(p.quad_source + quad) * 2 + second;
-	if(p.tri_opacity) {
-		f.opacity = __ldg(p.tri_opacity + f.prim);
-		f.col.w = f.col.w * f.opacity;
-	}
-	return f;
-}
 
 __device__ __forceinline__ uint32_t fragPrim(const FrameParams& p, const uint2* scratch, int band_cap,
 											 uint32_t val) {
@@ -456,23 +337,101 @@ __device__ __forceinline__ void forEachGroupFragment(const FrameParams& p, const
 	}
 }
 
-template <int MODE>
-__global__ void __launch_bounds__(RT, 1) rasterKernel(FrameParams p) {
+// Work sources of the raster kernel: the bins of one frame, or the bins of every view of a
+// batched frame.
+struct OneViewWork {
+	FrameParams p;
+	__device__ __forceinline__ const FrameParams& first() const { return p; }
+	__device__ __forceinline__ lucid_info* timerInfo() const { return p.info; }
+	// thread 0: next bin of the work list (HIGH, LOW, EMPTY), -1 when done
+	__device__ __forceinline__ void next(RasterSmem& s) const {
+		uint32_t w = atomicAdd(&p.info->raster_work_counter, 1u);
+		s.bin = w < uint32_t(p.bin_count) ? int(p.raster_work[w]) : -1;
+		s.view = 0;
+	}
+	__device__ __forceinline__ const FrameParams& view(RasterSmem&) const { return p; }
+};
+
+// All views' HIGH bins are handed out first (view by view), then the LOW bins, then the EMPTY
+// ones, so the heaviest bins of every view start early.
+struct BatchWork {
+	const FrameParams* views;
+	int num_views;
+	uint32_t* counter;       // work items handed out
+	const int* level_prefix; // [3][num_views + 1] bins of each level (HIGH, LOW, EMPTY) before view v
+	__device__ __forceinline__ const FrameParams& first() const { return views[0]; }
+	__device__ __forceinline__ lucid_info* timerInfo() const { return nullptr; }
+	__device__ __forceinline__ void next(RasterSmem& s) const {
+		const int w = int(atomicAdd(counter, 1u));
+		const int nv1 = num_views + 1;
+		int bin = -1, view = -1, base = 0;
+		for(int L = 0; L < 3; L++) {
+			const int* pre = level_prefix + L * nv1;
+			const int n = pre[num_views];
+			if(w < base + n) {
+				const int j = w - base;
+				int lo = 0, hi = num_views - 1;
+				while(lo < hi) {
+					int mid = (lo + hi + 1) >> 1;
+					if(pre[mid] <= j)
+						lo = mid;
+					else
+						hi = mid - 1;
+				}
+				const int* ph = level_prefix, *pl = level_prefix + nv1;
+				const int nhigh = ph[lo + 1] - ph[lo], nlow = pl[lo + 1] - pl[lo];
+				const int k = j - pre[lo];
+				const int pos = L == 0 ? k : L == 1 ? nhigh + k : nhigh + nlow + k;
+				view = lo;
+				bin = int(views[lo].raster_work[pos]);
+				break;
+			}
+			base += n;
+		}
+		s.bin = bin;
+		s.view = view;
+	}
+	// called by every thread after the barrier that follows next()
+	__device__ __forceinline__ const FrameParams& view(RasterSmem& s) const {
+		if(s.view != s.loaded_view) {
+			const uint32_t* src = reinterpret_cast<const uint32_t*>(views + s.view);
+			uint32_t* dst = reinterpret_cast<uint32_t*>(&s.view_params);
+			for(int i = threadIdx.x; i < int(sizeof(FrameParams) / 4); i += blockDim.x)
+				dst[i] = src[i];
+			__syncthreads();
+			if(threadIdx.x == 0)
+				s.loaded_view = s.view;
+		}
+		return s.view_params;
+	}
+};
+
+template <int MODE, class Work>
+__global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	RasterSmem& s = *reinterpret_cast<RasterSmem*>(smem_raw);
 	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-	const int band_cap = p.band_capacity;
-	uint2* scratch = p.band_scratch + size_t(blockIdx.x) * 8 * band_cap;
-	const float4 bg = make_float4(p.cfg.background_color[0], p.cfg.background_color[1],
-								  p.cfg.background_color[2], p.cfg.background_color[3]);
-	const bool additive = (p.flags & LUCID_OPT_ADDITIVE_BLENDING) != 0;
-	const bool alpha_threshold = (p.flags & LUCID_OPT_ALPHA_THRESHOLD) != 0;
-	const bool dump = p.dump_counts != nullptr;
+	// band scratch, its capacity and the option flags are the renderer's, shared by all views
+	const FrameParams& p_first = work.first();
+	const int band_cap = p_first.band_capacity;
+	uint2* scratch = p_first.band_scratch + size_t(blockIdx.x) * 8 * band_cap;
+	const uint32_t opt_flags = p_first.flags;
+	const bool additive = (opt_flags & LUCID_OPT_ADDITIVE_BLENDING) != 0;
+	const bool alpha_threshold = (opt_flags & LUCID_OPT_ALPHA_THRESHOLD) != 0;
+	if(tid == 0)
+		s.loaded_view = -1;
+	// the FP64 colour and backward raster passes of a differentiable frame run only when its
+	// fragment store overflowed (otherwise the pixel-parallel gradient kernels do the work)
+	if constexpr(MODE == kRasterStats || MODE == kRasterBackward) {
+		if(p_first.grad_state && *reinterpret_cast<volatile unsigned long long*>(p_first.grad_state) == 0ull)
+			return;
+	}
 	// Section timers (timers.glsl:9-39): thread 0 accumulates clock64 deltas between the
 	// CTA-wide barriers that separate the phases; units of 256 cycles in lucid_info.raster_timers:
 	// 0 row spans, 1 counts, 2 depth histograms, 3 window fragments, 4 sort, 5 shading,
 	// 6 blending, 7 output and bin fetch.
-	const bool timers = (p.flags & LUCID_OPT_TIMERS) != 0;
+	lucid_info* const timer_info = work.timerInfo();
+	const bool timers = (opt_flags & LUCID_OPT_TIMERS) != 0 && timer_info != nullptr;
 	long long tacc[8] = {0, 0, 0, 0, 0, 0, 0, 0}, tlast = timers ? clock64() : 0;
 #define RASTER_TIMER(i)                                                                            \
 	do {                                                                                           \
@@ -485,8 +444,7 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(FrameParams p) {
 
 	while(true) {
 		if(tid == 0) {
-			uint32_t w = atomicAdd(&p.info->raster_work_counter, 1u);
-			s.bin = w < uint32_t(p.bin_count) ? int(p.raster_work[w]) : -1;
+			work.next(s);
 			s.stat_hbt = 0;
 		}
 		if(tid < 8)
@@ -498,6 +456,10 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(FrameParams p) {
 		const int bin = s.bin;
 		if(bin < 0)
 			break;
+		const FrameParams& p = work.view(s);
+		const float4 bg = make_float4(p.cfg.background_color[0], p.cfg.background_color[1],
+									  p.cfg.background_color[2], p.cfg.background_color[3]);
+		const bool dump = p.dump_counts != nullptr;
 		const int bx = bin % p.bin_count_x, by = bin / p.bin_count_x;
 		const int bin_x = bx * kBinSize, bin_y = by * kBinSize;
 		const int vis_w = p.width - bin_x, vis_h = p.height - bin_y;
@@ -607,7 +569,30 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(FrameParams p) {
 			if(tid == 0)
 				s.eff_prefix[1024] = total;
 			int frags;
-			blockExclusiveScan(c0 + c1, s.scan_tmp, &frags);
+			const int foff = blockExclusiveScan(c0 + c1, s.scan_tmp, &frags);
+			if constexpr(MODE == kRasterStore) {
+				// the bin's slice of the fragment store; per pixel its offset and count
+				if(tid == 0) {
+					unsigned long long base = atomicAdd(&p.grad_state[1], (unsigned long long)frags);
+					s.store_ok = base + (unsigned long long)frags <= p.grad_capacity;
+					if(!s.store_ok)
+						atomicExch(&p.grad_state[0], 1ull);
+					s.store_base = base;
+				}
+				__syncthreads();
+				if(s.store_ok) {
+					const uint32_t base = uint32_t(s.store_base);
+					const int cs[2] = {c0, c1};
+					for(int k = 0; k < 2; k++) {
+						const int pl = 2 * tid + k;
+						const int px = bin_x + (pl & 31), py = bin_y + (pl >> 5);
+						if(px < p.width && py < p.height) {
+							p.grad_px_off[size_t(py) * p.width + px] = base + uint32_t(foff + (k ? c0 : 0));
+							p.grad_px_cnt[size_t(py) * p.width + px] = uint32_t(cs[k]);
+						}
+					}
+				}
+			}
 			int mx = max(c0, c1);
 #pragma unroll
 			for(int o = 16; o > 0; o >>= 1)
@@ -938,9 +923,30 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(FrameParams p) {
 				__syncthreads();
 				RASTER_TIMER(1);
 
-				// C6. shade in batches, blend sequentially per pixel
+				// C6. shade in batches, blend sequentially per pixel (store mode: copy the sorted
+				// window to the pixel's store slice, one warp per pixel)
 				float4* stage = reinterpret_cast<float4*>(&s.kv[cur ^ 1][0][0]);
-				while(true) {
+				if constexpr(MODE == kRasterStore) {
+					if(s.store_ok) {
+						for(int tp = warp; tp < npix; tp += NW) {
+							if(s.px_state[tp] != 0 || s.px_cut[tp] < 0)
+								continue;
+							const int pl = p0 + tp;
+							const int px = bin_x + (pl & 31), py = bin_y + (pl >> 5);
+							if(px >= p.width || py >= p.height)
+								continue;
+							const uint32_t dst = p.grad_px_off[size_t(py) * p.width + px] + uint32_t(s.px_done[tp]);
+							const int wb = s.px_wbase[tp], wc = s.px_wcnt[tp];
+							for(int k = lane; k < wc; k += 32) {
+								uint32_t v = V[wb + k];
+								uint32_t band = (v >> 8) & 7u, eslot = v >> 11;
+								p.grad_tris[dst + k] = entryTri(scratch[size_t(band) * band_cap + eslot]);
+							}
+						}
+					}
+					__syncthreads();
+				}
+				while(MODE != kRasterStore) {
 					if constexpr(MODE != kRasterBackward) {
 #pragma unroll 2
 						for(int slot = tid; slot < npix * batch; slot += RT) {
@@ -985,25 +991,25 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(FrameParams p) {
 								const float cc[3] = {c.x, c.y, c.z};
 								double da = 0.0;
 								float dc[3];
-								const double inv = 1.0 - double(a);
+								const double inv = 1.0 - double(a); // exact: a has a 24-bit mantissa
+								const double rinv = inv != 0.0 ? 1.0 / inv : 0.0;
 								for(int ch = 0; ch < 3; ch++) {
 									acc64[ch] += double(ca[ch]) * T64;
 									double behind = c64[ch] - acc64[ch];
 									dc[ch] = float(double(grad[ch]) * double(a) * T64);
-									double term = double(cc[ch]) * T64;
-									if(inv != 0.0)
-										term -= behind / inv;
+									double term = double(cc[ch]) * T64 - behind * rinv;
 									da += double(grad[ch]) * term;
 								}
 								T64 *= inv;
 								if(p.dvertex_rgba && fs.has_vc && p.color_format == LUCID_COLOR_RGBA32F) {
-									const float inst[4] = {fs.inst.x, fs.inst.y, fs.inst.z, fs.inst.w};
+									// one vector reduction per vertex (RGBA rows are 16-byte aligned)
 									const float dalpha = float(da) * fs.opacity;
 									for(int k = 0; k < 3; k++) {
-										float* dst = p.dvertex_rgba + size_t(fs.vid[k]) * 4;
-										for(int ch = 0; ch < 3; ch++)
-											atomicAdd(dst + ch, inst[ch] * fs.wgt[k] * dc[ch]);
-										atomicAdd(dst + 3, inst[3] * fs.wgt[k] * dalpha);
+										float4* dst = reinterpret_cast<float4*>(p.dvertex_rgba) + fs.vid[k];
+										atomicAdd(dst, make_float4(fs.inst.x * fs.wgt[k] * dc[0],
+																   fs.inst.y * fs.wgt[k] * dc[1],
+																   fs.inst.z * fs.wgt[k] * dc[2],
+																   fs.inst.w * fs.wgt[k] * dalpha));
 									}
 								}
 								if(p.dtri_opacity && p.tri_opacity)
@@ -1068,7 +1074,7 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(FrameParams p) {
 			}
 
 			// C7. output
-			if(t < npix && MODE != kRasterBackward) {
+			if(t < npix && MODE != kRasterBackward && MODE != kRasterStore) {
 				int pl = p0 + t;
 				int px = bin_x + (pl & 31), py = bin_y + (pl >> 5);
 				float T = s.px_T[t];
@@ -1107,29 +1113,66 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(FrameParams p) {
 	}
 	if(timers && tid == 0)
 		for(int i = 0; i < 8; i++)
-			atomicAdd(&p.info->raster_timers[i], uint32_t(tacc[i] >> 8));
+			atomicAdd(&timer_info->raster_timers[i], uint32_t(tacc[i] >> 8));
 #undef RASTER_TIMER
 }
 
 void launchRaster(const FrameParams& p, int num_ctas, cudaStream_t stream, int mode) {
-	if(mode == kRasterStats)
-		rasterKernel<kRasterStats><<<num_ctas, RT, sizeof(RasterSmem), stream>>>(p);
+	const OneViewWork w{p};
+	if(mode == kRasterStore)
+		rasterKernel<kRasterStore><<<num_ctas, RT, sizeof(RasterSmem), stream>>>(w);
+	else if(mode == kRasterStats)
+		rasterKernel<kRasterStats><<<num_ctas, RT, sizeof(RasterSmem), stream>>>(w);
 	else if(mode == kRasterBackward)
-		rasterKernel<kRasterBackward><<<num_ctas, RT, sizeof(RasterSmem), stream>>>(p);
+		rasterKernel<kRasterBackward><<<num_ctas, RT, sizeof(RasterSmem), stream>>>(w);
 	else
-		rasterKernel<kRasterForward><<<num_ctas, RT, sizeof(RasterSmem), stream>>>(p);
+		rasterKernel<kRasterForward><<<num_ctas, RT, sizeof(RasterSmem), stream>>>(w);
+}
+
+// One CTA: bins of each level per view (from the categorizer's counts) as prefix sums over
+// the views, and the work counter of the batched raster pass reset.
+__global__ void __launch_bounds__(kMaxBatchViews) batchPlanKernel(const FrameParams* views, int num_views,
+																   int* level_prefix, uint32_t* counter) {
+	__shared__ int s_scan[kMaxBatchViews / 32 + 1];
+	const int v = threadIdx.x;
+	const int levels[3] = {LUCID_BIN_LEVEL_HIGH, LUCID_BIN_LEVEL_LOW, LUCID_BIN_LEVEL_EMPTY};
+	for(int L = 0; L < 3; L++) {
+		int n = v < num_views ? int(views[v].info->bin_level_counts[levels[L]]) : 0;
+		int total;
+		int off = blockExclusiveScan(n, s_scan, &total);
+		if(v < num_views)
+			level_prefix[L * (num_views + 1) + v] = off;
+		if(v == 0)
+			level_prefix[L * (num_views + 1) + num_views] = total;
+	}
+	if(v == 0)
+		*counter = 0;
+}
+
+void launchRasterBatch(const FrameParams* views_dev, int num_views, int* level_prefix, uint32_t* counter,
+					   int num_ctas, cudaStream_t stream) {
+	batchPlanKernel<<<1, kMaxBatchViews, 0, stream>>>(views_dev, num_views, level_prefix, counter);
+	const BatchWork w{views_dev, num_views, counter, level_prefix};
+	rasterKernel<kRasterForward><<<num_ctas, RT, sizeof(RasterSmem), stream>>>(w);
 }
 
 cudaError_t configureRasterKernel() {
 	cudaError_t err;
-	if((err = cudaFuncSetAttribute(rasterKernel<kRasterForward>,
-								   cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(RasterSmem)))) != cudaSuccess)
+	const int bytes = int(sizeof(RasterSmem));
+	if((err = cudaFuncSetAttribute(rasterKernel<kRasterForward, OneViewWork>,
+								   cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess)
 		return err;
-	if((err = cudaFuncSetAttribute(rasterKernel<kRasterStats>,
-								   cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(RasterSmem)))) != cudaSuccess)
+	if((err = cudaFuncSetAttribute(rasterKernel<kRasterStats, OneViewWork>,
+								   cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess)
 		return err;
-	return cudaFuncSetAttribute(rasterKernel<kRasterBackward>,
-								cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(RasterSmem)));
+	if((err = cudaFuncSetAttribute(rasterKernel<kRasterBackward, OneViewWork>,
+								   cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess)
+		return err;
+	if((err = cudaFuncSetAttribute(rasterKernel<kRasterStore, OneViewWork>,
+								   cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) != cudaSuccess)
+		return err;
+	return cudaFuncSetAttribute(rasterKernel<kRasterForward, BatchWork>,
+								cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
 } // namespace lucid

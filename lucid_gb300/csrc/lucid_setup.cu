@@ -296,8 +296,10 @@ __device__ __forceinline__ void loadQuadIndices(const FrameParams& p, int inst, 
 // ---------------------------------------------------------------------------------------------
 // Kernels
 
-__global__ void __launch_bounds__(1024) setupPrepKernel(FrameParams p) {
+template <class Src> __global__ void __launch_bounds__(1024) setupPrepKernel(Src src) {
 	__shared__ int s_scan[33];
+	int cta, ncta;
+	const FrameParams& p = src.get(cta, ncta);
 	int n = p.num_instances;
 	int per = (n + blockDim.x - 1) / blockDim.x;
 	int beg = min(n, int(threadIdx.x) * per), end = min(n, beg + per);
@@ -324,12 +326,14 @@ __global__ void __launch_bounds__(1024) setupPrepKernel(FrameParams p) {
 		raiseError(p.info, LUCID_ERR_INSTANCE_QUADS, 0, 0, 1);
 }
 
-__global__ void __launch_bounds__(kSetupThreads) setupClassifyKernel(FrameParams p) {
+template <class Src> __global__ void __launch_bounds__(kSetupThreads) setupClassifyKernel(Src src) {
 	__shared__ int s_counts[2 + LUCID_REJECTION_TYPE_COUNT];
+	int cta, ncta;
+	const FrameParams& p = src.get(cta, ncta);
 	if(threadIdx.x < 2 + LUCID_REJECTION_TYPE_COUNT)
 		s_counts[threadIdx.x] = 0;
 	__syncthreads();
-	int q = blockIdx.x * blockDim.x + threadIdx.x;
+	int q = cta * blockDim.x + threadIdx.x;
 	int cls = -1;
 	if(q < p.num_quads) {
 		int inst = findInstance(p.inst_offsets, p.num_instances, q);
@@ -345,13 +349,15 @@ __global__ void __launch_bounds__(kSetupThreads) setupClassifyKernel(FrameParams
 	int nsmall = __syncthreads_count(cls == 0);
 	int nlarge = __syncthreads_count(cls == 1);
 	if(threadIdx.x == 0)
-		p.setup_cta_counts[blockIdx.x] = make_int4(nsmall, nlarge, 0, 0);
+		p.setup_cta_counts[cta] = make_int4(nsmall, nlarge, 0, 0);
 	if(threadIdx.x < LUCID_REJECTION_TYPE_COUNT && s_counts[2 + threadIdx.x] > 0)
 		atomicAdd(&p.info->num_rejected_quads[threadIdx.x], uint32_t(s_counts[2 + threadIdx.x]));
 }
 
-__global__ void __launch_bounds__(1024) setupScanKernel(FrameParams p) {
+template <class Src> __global__ void __launch_bounds__(1024) setupScanKernel(Src src) {
 	__shared__ int s_scan[33];
+	int cta, ncta;
+	const FrameParams& p = src.get(cta, ncta);
 	int n = p.num_setup_ctas;
 	int per = (n + blockDim.x - 1) / blockDim.x;
 	int beg = min(n, int(threadIdx.x) * per), end = min(n, beg + per);
@@ -378,14 +384,16 @@ __global__ void __launch_bounds__(1024) setupScanKernel(FrameParams p) {
 	}
 }
 
-__global__ void __launch_bounds__(kSetupThreads) setupStoreKernel(FrameParams p) {
+template <class Src> __global__ void __launch_bounds__(kSetupThreads) setupStoreKernel(Src src) {
 	__shared__ int s_scan[kSetupThreads / 32 + 1];
-	int q = blockIdx.x * blockDim.x + threadIdx.x;
+	int cta, ncta;
+	const FrameParams& p = src.get(cta, ncta);
+	int q = cta * blockDim.x + threadIdx.x;
 	uint4 rec = make_uint4(0, 0, 0, 0);
 	if(q < p.num_quads)
 		rec = p.quad_class[q];
 	int cls = int(rec.w & 0xffu) - 1;
-	int4 base = p.setup_cta_offsets[blockIdx.x];
+	int4 base = p.setup_cta_offsets[cta];
 	int rs = blockExclusiveScan(cls == 0 ? 1 : 0, s_scan, (int*)nullptr);
 	int rl = blockExclusiveScan(cls == 1 ? 1 : 0, s_scan, (int*)nullptr);
 	if(cls < 0)
@@ -438,12 +446,23 @@ __global__ void __launch_bounds__(kSetupThreads) setupStoreKernel(FrameParams p)
 // Launchers
 
 void launchSetup(const FrameParams& p, cudaStream_t stream) {
-	setupPrepKernel<<<1, 1024, 0, stream>>>(p);
+	const OneView v{p};
+	setupPrepKernel<<<1, 1024, 0, stream>>>(v);
 	if(p.num_quads > 0) {
-		setupClassifyKernel<<<p.num_setup_ctas, kSetupThreads, 0, stream>>>(p);
-		setupScanKernel<<<1, 1024, 0, stream>>>(p);
-		setupStoreKernel<<<p.num_setup_ctas, kSetupThreads, 0, stream>>>(p);
+		setupClassifyKernel<<<p.num_setup_ctas, kSetupThreads, 0, stream>>>(v);
+		setupScanKernel<<<1, 1024, 0, stream>>>(v);
+		setupStoreKernel<<<p.num_setup_ctas, kSetupThreads, 0, stream>>>(v);
 	}
+}
+
+void launchSetupBatch(const BatchViews& per_view, const BatchViews& setup_ctas, cudaStream_t stream) {
+	setupPrepKernel<<<per_view.num_views, 1024, 0, stream>>>(per_view);
+	const int n = setup_ctas.cta_off[setup_ctas.num_views];
+	if(n > 0)
+		setupClassifyKernel<<<n, kSetupThreads, 0, stream>>>(setup_ctas);
+	setupScanKernel<<<per_view.num_views, 1024, 0, stream>>>(per_view);
+	if(n > 0)
+		setupStoreKernel<<<n, kSetupThreads, 0, stream>>>(setup_ctas);
 }
 
 } // namespace lucid

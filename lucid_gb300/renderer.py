@@ -83,7 +83,8 @@ class LucidRenderer:
     def __init__(self, width: int, height: int, *, max_input_quads: int | None = None,
                  max_visible_quads: int | None = None, max_bin_refs: int | None = None,
                  band_capacity: int | None = None, flags: int = 0, low_high_threshold: int = 1024,
-                 raster_ctas_per_sm: int = 0, binning_ctas: int = 0, max_views: int = 1):
+                 raster_ctas_per_sm: int = 0, binning_ctas: int = 0, max_views: int = 1,
+                 grad_store_fragments: int = 0):
         if not torch.cuda.is_available():
             raise RuntimeError("lucid_gb300 needs a CUDA device")
         self.lib = _lib.load()
@@ -101,6 +102,7 @@ class LucidRenderer:
         o.raster_ctas_per_sm = int(raster_ctas_per_sm)
         o.binning_ctas = int(binning_ctas)
         o.max_views = int(max_views)
+        o.grad_store_fragments = int(grad_store_fragments)
         self.options = o
         self.width, self.height = int(width), int(height)
         self.bin_count_x = (self.width + 31) // 32
@@ -174,6 +176,27 @@ class LucidRenderer:
         return out, counts, prims[..., :max_per_pixel]
 
     # -- info / statistics ------------------------------------------------------------------
+    def render_batch(self, frames, outs=None, stream=None):
+        """Renders every (frame, width, height) of `frames` with lucid_render_batch; returns the
+        output images (allocated unless `outs` is given)."""
+        n = len(frames)
+        if outs is None:
+            outs = [torch.empty((h, w, 4), dtype=torch.float32, device="cuda") for _, w, h in frames]
+        views = (_lib.ViewC * n)()
+        for i, ((frame, w, h), out) in enumerate(zip(frames, outs)):
+            views[i].width, views[i].height = int(w), int(h)
+            views[i].inputs = frame.c_struct()
+            views[i].out_rgba = out.data_ptr()
+        self._batch_keep = (frames, outs)
+        check(self.lib.lucid_render_batch(self.handle, views, n, _stream_ptr(stream)), "lucid_render_batch")
+        return outs
+
+    def batch_info(self, view: int, stream=None):
+        info = _lib.Info()
+        check(self.lib.lucid_get_batch_info(self.handle, int(view), ctypes.byref(info), _stream_ptr(stream)),
+              "lucid_get_batch_info")
+        return info
+
     def info(self, stream=None):
         info = _lib.Info()
         counters = np.zeros(10 * self.num_bins, np.uint32)

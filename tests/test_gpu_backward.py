@@ -25,12 +25,12 @@ def rel_err(g, ref):
     return np.abs(g - ref) / scale
 
 
-def gpu_grads(sc, target):
+def gpu_grads(sc, target, grad_store_fragments=0):
     import torch
     from lucid_gb300 import autograd
     from lucid_gb300.renderer import FrameInputs, LucidRenderer
     r = LucidRenderer(sc.width, sc.height, max_input_quads=max(1024, sc.num_quads),
-                      max_visible_quads=max(1024, sc.num_quads))
+                      max_visible_quads=max(1024, sc.num_quads), grad_store_fragments=grad_store_fragments)
     frame = FrameInputs.from_scene(sc)
     vc = torch.from_numpy(sc.colors.astype(np.float32)).cuda().requires_grad_(True)
     op = torch.from_numpy(sc.tri_opacity.astype(np.float32)).cuda().requires_grad_(True)
@@ -92,6 +92,20 @@ def test_backward_matches_fp64_analytic_and_fd(gpu, oracle, w, h, n, seed):
     got = np.concatenate([g["dvc"].ravel()[iv], g["dop"][io]])
     err = rel_err(got, ref)
     assert err.max() <= TOL, (err.max(), np.argmax(err))
+
+
+@pytest.mark.parametrize("store", [-1, 1000])
+def test_backward_without_fragment_store(gpu, oracle, store):
+    """No fragment store (-1), or one too small for the frame (1000 fragments): the raster
+    pass recomputes the fragment lists; image and gradients agree with the store path."""
+    sc, pert = scene_and_target(96, 64, 1500, 8, area_median=150.0)
+    psc = scenes.Scene(**{**sc.__dict__, "colors": pert.astype(np.float32)})
+    target = oracle.run(psc)["image"]
+    a = gpu_grads(sc, target)
+    b = gpu_grads(sc, target, grad_store_fragments=store)
+    np.testing.assert_array_equal(a["image"], b["image"])
+    assert rel_err(b["dvc"].ravel(), a["dvc"].ravel()).max() <= 1e-5
+    assert rel_err(b["dop"], a["dop"]).max() <= 1e-5
 
 
 def test_backward_rejects_unsupported(gpu):
