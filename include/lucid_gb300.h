@@ -197,6 +197,9 @@ typedef struct lucid_info {
 #define LUCID_OPT_ADDITIVE_BLENDING 0x02u /* out += rgb*a (shading.glsl:276-277)               */
 #define LUCID_OPT_ALPHA_THRESHOLD 0x04u   /* stop a pixel once T < 1/128 (shading.glsl:62)     */
 #define LUCID_OPT_VISUALIZE_ERRORS 0x08u  /* reserved (reference-order mode only)              */
+#define LUCID_OPT_PIXEL_BLEND 0x10u       /* raster pass stores each pixel's sorted fragment
+                                           * list; a pixel-parallel kernel shades and blends it
+                                           * (same image bits; lucid_autotune picks it per scene) */
 
 typedef struct lucid_options {
 	uint32_t flags;            /* LUCID_OPT_*                                                  */
@@ -383,11 +386,26 @@ lucid_status lucid_render_batch(lucid_renderer* renderer, const lucid_view* view
 /* Copies (synchronising `stream`) the lucid_info of view `view` of the last lucid_render_batch. */
 lucid_status lucid_get_batch_info(lucid_renderer* renderer, int32_t view, lucid_info* out, void* stream);
 
-/* Picks raster launch parameters by timing candidate configurations on `inputs`; stores the
- * winner in the renderer and returns it in *out_ctas_per_sm / *out_low_high_threshold. */
+/* Result of lucid_autotune. */
+typedef struct lucid_tuning {
+	uint32_t pixel_blend;       /* 1: LUCID_OPT_PIXEL_BLEND chosen                               */
+	int32_t low_high_threshold; /* bins with >= this many tris are rastered first (HIGH)        */
+	int32_t binning_ctas;       /* CTAs of the bin counter / dispatcher                         */
+	int32_t num_candidates;     /* configurations timed                                         */
+	float frame_ms;             /* median frame time of the winner                               */
+	float default_ms;           /* median frame time of the renderer's options before tuning     */
+	int32_t reserved[2];
+} lucid_tuning;
+
+/* Autotuner (no reference counterpart): times lucid_render of `inputs` into scratch_rgba
+ * (device, width*height*4 floats) under candidate configurations, by coordinate descent over
+ * the blend strategy (raster-pass blend or LUCID_OPT_PIXEL_BLEND), the LOW/HIGH threshold
+ * (256, 1024, 4096) and the binning CTAs (1 or 2 per SM, within options.binning_ctas); CUDA
+ * events on `stream`, median of 3 frames after one warm-up frame each. The winner is stored in
+ * the renderer's options and returned in *out (may be NULL). Synchronous. Bin size is fixed at
+ * 32 (the reference's only size); raster CTAs are one per SM (shared memory). */
 lucid_status lucid_autotune(lucid_renderer* renderer, const lucid_frame_inputs* inputs,
-							float* scratch_rgba, int32_t* out_ctas_per_sm,
-							int32_t* out_low_high_threshold, void* stream);
+							float* scratch_rgba, lucid_tuning* out, void* stream);
 
 /* ---------------------------------------------------------------------------------------- */
 /* Binning without allocation. No counterpart in the reference.

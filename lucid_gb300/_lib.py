@@ -23,6 +23,7 @@ ERR_NAMES = {0: "none", 1: "visible quads", 2: "bin refs", 3: "band entries",
 
 # render option flags
 OPT_TIMERS, OPT_ADDITIVE_BLENDING, OPT_ALPHA_THRESHOLD, OPT_VISUALIZE_ERRORS = 1, 2, 4, 8
+OPT_PIXEL_BLEND = 16
 
 # internal buffers of lucid_download_buffer
 BUF_QUAD_AABBS, BUF_TRI_BARY, BUF_TRI_SCAN, BUF_TRI_DEPTH, BUF_QUAD_COLORS = 0, 1, 2, 3, 4
@@ -79,6 +80,12 @@ class CameraC(ctypes.Structure):
                 ("far_plane", c_float)]
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [("pixel_blend", c_uint32), ("low_high_threshold", c_int32), ("binning_ctas", c_int32),
+                ("num_candidates", c_int32), ("frame_ms", ctypes.c_float), ("default_ms", ctypes.c_float),
+                ("reserved", c_int32 * 2)]
+
+
 class ViewC(ctypes.Structure):
     _fields_ = [("width", c_int32), ("height", c_int32), ("inputs", FrameInputsC),
                 ("out_rgba", c_void_p)]
@@ -113,7 +120,7 @@ SIGNATURES = [
     ("lucid_render_batch", c_int32, [c_void_p, ctypes.POINTER(ViewC), c_int32, c_void_p]),
     ("lucid_get_batch_info", c_int32, [c_void_p, c_int32, ctypes.POINTER(Info), c_void_p]),
     ("lucid_autotune", c_int32, [c_void_p, ctypes.POINTER(FrameInputsC), c_void_p,
-                                 ctypes.POINTER(c_int32), ctypes.POINTER(c_int32), c_void_p]),
+                                 ctypes.POINTER(Tuning), c_void_p]),
     ("lucid_bin_noalloc", c_int32, [c_void_p, c_void_p, c_int32, c_int32, c_int32, c_int32,
                                     c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_int32,
                                     c_void_p, c_void_p]),

@@ -6,6 +6,7 @@
 // sizes never depend on device-side counts (fixed or persistent grids read the counts on the
 // device), so a frame needs no indirect dispatch and can be captured in a CUDA graph.
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -67,6 +68,7 @@ struct lucid_renderer {
 	int device, num_sms;
 	int raster_ctas;
 	int setup_ctas_max;
+	int binning_ctas_alloc; // CTAs the binning histogram scratch is sized for
 	std::vector<void*> allocations;
 
 	// buffers
@@ -407,6 +409,7 @@ extern "C" lucid_status lucid_create(const lucid_options* options, int32_t width
 	if(r->opts.binning_ctas <= 0)
 		r->opts.binning_ctas = 2 * r->num_sms;
 	r->opts.binning_ctas = std::min(r->opts.binning_ctas, 4096);
+	r->binning_ctas_alloc = r->opts.binning_ctas;
 	err = configureRasterKernel();
 	if(err != cudaSuccess)
 		return bail(cudaFail(err, "configure raster kernel"));
@@ -512,6 +515,46 @@ extern "C" lucid_status lucid_bin_dispatch(lucid_renderer* r, void* stream) {
 	return checkLaunch("bin dispatch");
 }
 
+static lucid_status ensureGradStore(lucid_renderer* r, cudaStream_t s);
+static lucid_status ensureStoreBuffers(lucid_renderer* r);
+
+// The raster pass in store mode followed by the pixel-parallel blend; when the store cannot
+// hold the frame, the raster pass's own blend runs instead (chosen on the device).
+static lucid_status rasterPixelBlend(lucid_renderer* r, FrameParams p, cudaStream_t s) {
+	lucid_status st;
+	if((st = ensureStoreBuffers(r)) != LUCID_OK || (st = ensureGradStore(r, s)) != LUCID_OK)
+		return st;
+	p.grad_tris = r->grad_tris;
+	p.grad_px_off = r->grad_px_off;
+	p.grad_px_cnt = r->grad_px_cnt;
+	p.grad_state = r->grad_state;
+	p.grad_capacity = r->grad_capacity;
+	LUCID_CUDA_TRY(cudaMemsetAsync(r->grad_state, 0, 16, s));
+	if(r->grad_capacity == 0)
+		LUCID_CUDA_TRY(cudaMemsetAsync(r->grad_state, 1, 8, s));
+	LUCID_CUDA_TRY(cudaMemsetAsync(r->grad_px_cnt, 0, size_t(r->width) * r->height * 4, s));
+	if((st = resetRasterCounters(r, s)) != LUCID_OK)
+		return st;
+	if(r->grad_capacity > 0) {
+		launchRaster(p, r->raster_ctas, s, kRasterStore);
+		if((st = checkLaunch("raster (store)")) != LUCID_OK)
+			return st;
+	}
+	LUCID_CUDA_TRY(cudaMemsetAsync(&r->info()->raster_work_counter, 0, 4, s));
+	launchRaster(p, r->raster_ctas, s, kRasterForward);
+	if((st = checkLaunch("raster")) != LUCID_OK)
+		return st;
+	launchBlendPixels(p, s);
+	if((st = checkLaunch("pixel blend")) != LUCID_OK)
+		return st;
+	if(r->grad_capacity > 0 && r->opts.grad_store_fragments == 0) {
+		LUCID_CUDA_TRY(cudaMemcpyAsync(r->grad_need_host, &r->grad_state[1], 8, cudaMemcpyDeviceToHost, s));
+		LUCID_CUDA_TRY(cudaEventRecord(r->grad_need_event, s));
+		r->grad_need_pending = true;
+	}
+	return LUCID_OK;
+}
+
 static lucid_status rasterImpl(lucid_renderer* r, const lucid_frame_inputs* in, float* out,
 							   int* dump_counts, int* dump_prims, int dump_max, cudaStream_t s) {
 	if(!r || !r->have_frame)
@@ -535,6 +578,8 @@ static lucid_status rasterImpl(lucid_renderer* r, const lucid_frame_inputs* in, 
 	p.dump_counts = dump_counts;
 	p.dump_prims = dump_prims;
 	p.dump_max = dump_max;
+	if((r->opts.flags & LUCID_OPT_PIXEL_BLEND) && !dump_counts)
+		return rasterPixelBlend(r, p, s);
 	if((st = resetRasterCounters(r, s)) != LUCID_OK)
 		return st;
 	launchRaster(p, r->raster_ctas, s);
@@ -644,9 +689,23 @@ extern "C" lucid_status lucid_raster_dump(lucid_renderer* r, const lucid_frame_i
 	return st;
 }
 
-namespace {
+// Per-pixel offsets / counts and the state words of the fragment store (allocated once).
+static lucid_status ensureStoreBuffers(lucid_renderer* r) {
+	if(r->grad_state)
+		return LUCID_OK;
+	const size_t npix = size_t(r->width) * r->height;
+	lucid_status st;
+	if((st = allocate(r, &r->grad_px_off, npix)) != LUCID_OK || (st = allocate(r, &r->grad_px_cnt, npix)) != LUCID_OK)
+		return st;
+	cudaError_t err = cudaHostAlloc(reinterpret_cast<void**>(&r->grad_need_host), 8, cudaHostAllocDefault);
+	if(err == cudaSuccess)
+		err = cudaEventCreateWithFlags(&r->grad_need_event, cudaEventDisableTiming);
+	if(err != cudaSuccess)
+		return cudaFail(err, "fragment store host state");
+	return allocate(r, &r->grad_state, 2);
+}
 
-lucid_status checkGradInputs(lucid_renderer* r, const lucid_frame_inputs* in) {
+static lucid_status checkGradInputs(lucid_renderer* r, const lucid_frame_inputs* in) {
 	lucid_status st = validateInputs(r, in);
 	if(st != LUCID_OK)
 		return st;
@@ -656,23 +715,15 @@ lucid_status checkGradInputs(lucid_renderer* r, const lucid_frame_inputs* in) {
 		const size_t npix = size_t(r->width) * r->height;
 		if((st = allocate(r, &r->px_color64, npix * 3)) != LUCID_OK ||
 		   (st = allocate(r, &r->px_color32, npix * 3)) != LUCID_OK ||
-		   (st = allocate(r, &r->stats_image, npix * 4)) != LUCID_OK ||
-		   (st = allocate(r, &r->grad_px_off, npix)) != LUCID_OK ||
-		   (st = allocate(r, &r->grad_px_cnt, npix)) != LUCID_OK ||
-		   (st = allocate(r, &r->grad_state, 2)) != LUCID_OK)
+		   (st = allocate(r, &r->stats_image, npix * 4)) != LUCID_OK)
 			return st;
-		cudaError_t err = cudaHostAlloc(reinterpret_cast<void**>(&r->grad_need_host), 8, cudaHostAllocDefault);
-		if(err == cudaSuccess)
-			err = cudaEventCreateWithFlags(&r->grad_need_event, cudaEventDisableTiming);
-		if(err != cudaSuccess)
-			return cudaFail(err, "gradient pass host state");
 	}
-	return LUCID_OK;
+	return ensureStoreBuffers(r);
 }
 
 // Sizes the fragment store: a fixed capacity, none, or (automatic) at least 2^25 fragments and
 // 1.25x the fragments of the last differentiable frame once that count is known on the host.
-lucid_status ensureGradStore(lucid_renderer* r, cudaStream_t s) {
+static lucid_status ensureGradStore(lucid_renderer* r, cudaStream_t s) {
 	const int32_t opt = r->opts.grad_store_fragments;
 	size_t want = r->grad_capacity;
 	if(opt > 0) {
@@ -702,13 +753,15 @@ lucid_status ensureGradStore(lucid_renderer* r, cudaStream_t s) {
 		cudaError_t err = cudaMalloc(&r->grad_tris, want * sizeof(uint32_t));
 		if(err != cudaSuccess) {
 			cudaGetLastError();
-			r->grad_tris = nullptr; // no store: the backward pass recomputes the fragment lists
+			r->grad_tris = nullptr; // no store: the raster pass recomputes the fragment lists
 			return LUCID_OK;
 		}
 		r->grad_capacity = want;
 	}
 	return LUCID_OK;
 }
+
+namespace {
 
 FrameParams gradParams(lucid_renderer* r) {
 	FrameParams p = r->last;
@@ -835,6 +888,7 @@ struct BatchPlan {
 	int max_bins = 0;
 	std::vector<FrameParams> params; // what params_pinned holds
 	std::vector<size_t> info_off;    // byte offset of each view's info block in `infos`
+	std::vector<int> binning_ctas;   // per view, fixed when the plan's buffers are sized
 	size_t info_bytes = 0;
 	BatchViews per_view{}, setup_map{}, binning_map{};
 	std::vector<void*> allocations;
@@ -940,7 +994,7 @@ void batchParams(lucid_renderer* r, BatchPlan* b, const lucid_view* views, std::
 		p.band_capacity = r->opts.band_capacity;
 		p.low_high_threshold = r->opts.low_high_threshold;
 		p.num_setup_ctas = viewSetupCtas(nq);
-		p.num_binning_ctas = viewBinningCtas(r, nq);
+		p.num_binning_ctas = b->binning_ctas[size_t(v)];
 		p.flags = r->opts.flags & ~uint32_t(LUCID_OPT_TIMERS);
 		p.info = reinterpret_cast<lucid_info*>(b->infos + b->info_off[size_t(v)]);
 		p.counts = reinterpret_cast<uint32_t*>(b->infos + b->info_off[size_t(v)] + sizeof(lucid_info));
@@ -981,6 +1035,7 @@ lucid_status buildBatchPlan(lucid_renderer* r, const lucid_view* views, int n, s
 	b->num_views = n;
 	size_t quads = 0, insts = 0, setup_ctas = 0, hist = 0, bins = 0;
 	b->info_off.resize(size_t(n));
+	b->binning_ctas.resize(size_t(n));
 	for(int v = 0; v < n; v++) {
 		const int nq = views[v].inputs.num_quads;
 		const int vb = viewBins(views[v].width, views[v].height);
@@ -988,7 +1043,8 @@ lucid_status buildBatchPlan(lucid_renderer* r, const lucid_view* views, int n, s
 		quads += size_t(std::max(nq, 1));
 		insts += size_t(views[v].inputs.num_instances) + 1;
 		setup_ctas += size_t(std::max(viewSetupCtas(nq), 1));
-		hist += size_t(viewBinningCtas(r, nq)) * 2 * size_t(vb);
+		b->binning_ctas[size_t(v)] = viewBinningCtas(r, nq);
+		hist += size_t(b->binning_ctas[size_t(v)]) * 2 * size_t(vb);
 		bins += size_t(vb);
 		b->info_off[size_t(v)] = b->info_bytes;
 		b->info_bytes += (sizeof(lucid_info) + size_t(10) * vb * 4 + 255) & ~size_t(255);
@@ -1032,7 +1088,7 @@ lucid_status buildBatchPlan(lucid_renderer* r, const lucid_view* views, int n, s
 		const int nq = views[v].inputs.num_quads;
 		b->per_view.cta_off[v + 1] = v + 1;
 		b->setup_map.cta_off[v + 1] = b->setup_map.cta_off[v] + viewSetupCtas(nq);
-		b->binning_map.cta_off[v + 1] = b->binning_map.cta_off[v] + viewBinningCtas(r, nq);
+		b->binning_map.cta_off[v + 1] = b->binning_map.cta_off[v] + b->binning_ctas[size_t(v)];
 	}
 
 	// record the frame
@@ -1119,9 +1175,91 @@ extern "C" lucid_status lucid_get_batch_info(lucid_renderer* r, int32_t view, lu
 }
 
 extern "C" lucid_status lucid_autotune(lucid_renderer* r, const lucid_frame_inputs* in,
-									   float* scratch_rgba, int32_t* out_ctas_per_sm,
-									   int32_t* out_low_high_threshold, void* stream) {
-	(void)r, (void)in, (void)scratch_rgba, (void)out_ctas_per_sm, (void)out_low_high_threshold,
-		(void)stream;
-	return fail(LUCID_NOT_SUPPORTED, "lucid_autotune is not built yet");
+									   float* scratch_rgba, lucid_tuning* out, void* stream) {
+	if(!r || !scratch_rgba)
+		return fail(LUCID_INVALID_ARG, "lucid_autotune: renderer and scratch_rgba are required");
+	lucid_status st = validateInputs(r, in);
+	if(st != LUCID_OK)
+		return st;
+	cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+	cudaEvent_t e0, e1;
+	LUCID_CUDA_TRY(cudaEventCreate(&e0));
+	cudaError_t cerr = cudaEventCreate(&e1);
+	if(cerr != cudaSuccess) {
+		cudaEventDestroy(e0);
+		return cudaFail(cerr, "cudaEventCreate");
+	}
+	const lucid_options saved = r->opts;
+	int candidates = 0;
+	// median of 3 timed frames after one warm-up frame; < 0 on failure
+	auto timeFrame = [&](float& ms) -> lucid_status {
+		float t[3];
+		for(int i = 0; i < 4; i++) {
+			cudaEventRecord(e0, s);
+			lucid_status rs = lucid_render(r, in, scratch_rgba, stream);
+			if(rs != LUCID_OK)
+				return rs;
+			cudaEventRecord(e1, s);
+			cudaError_t err = cudaEventSynchronize(e1);
+			if(err != cudaSuccess)
+				return cudaFail(err, "autotune frame");
+			if(i > 0)
+				cudaEventElapsedTime(&t[i - 1], e0, e1);
+		}
+		std::sort(t, t + 3);
+		ms = t[1];
+		candidates++;
+		return LUCID_OK;
+	};
+	float best_ms = 0.0f, default_ms = 0.0f;
+	if((st = timeFrame(default_ms)) == LUCID_OK) {
+		best_ms = default_ms;
+		lucid_options best = r->opts;
+		auto tryOpts = [&](const lucid_options& o) -> lucid_status {
+			r->opts = o;
+			float ms = 0.0f;
+			lucid_status rs = timeFrame(ms);
+			if(rs == LUCID_OK && ms < best_ms)
+				best_ms = ms, best = o;
+			r->opts = best;
+			return rs;
+		};
+		// 1. blend strategy
+		lucid_options o = best;
+		o.flags ^= LUCID_OPT_PIXEL_BLEND;
+		st = tryOpts(o);
+		// 2. LOW/HIGH threshold (raster work order)
+		for(int th : {256, 1024, 4096}) {
+			if(st != LUCID_OK || th == best.low_high_threshold)
+				continue;
+			o = best;
+			o.low_high_threshold = th;
+			st = tryOpts(o);
+		}
+		// 3. binning CTAs (within what the histogram scratch is sized for)
+		for(int ctas : {r->num_sms, 2 * r->num_sms}) {
+			if(st != LUCID_OK || ctas == best.binning_ctas || ctas > r->binning_ctas_alloc)
+				continue;
+			o = best;
+			o.binning_ctas = ctas;
+			st = tryOpts(o);
+		}
+		r->opts = st == LUCID_OK ? best : saved;
+	}
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	if(st != LUCID_OK) {
+		r->opts = saved;
+		return st;
+	}
+	if(out) {
+		memset(out, 0, sizeof(*out));
+		out->pixel_blend = (r->opts.flags & LUCID_OPT_PIXEL_BLEND) ? 1u : 0u;
+		out->low_high_threshold = r->opts.low_high_threshold;
+		out->binning_ctas = r->opts.binning_ctas;
+		out->num_candidates = candidates;
+		out->frame_ms = best_ms;
+		out->default_ms = default_ms;
+	}
+	return LUCID_OK;
 }

@@ -16,7 +16,9 @@ void launchBinningBatch(const BatchViews& per_view, const BatchViews& binning_ct
 						cudaStream_t stream);
 void launchRasterBatch(const FrameParams* views_dev, int num_views, int* level_prefix, uint32_t* counter,
 					   int num_ctas, cudaStream_t stream);
-// Differentiable frames: pixel-parallel kernels over the fragment store.
+// Pixel-parallel kernels over the fragment store: the plain blend and the differentiable
+// frame's FP64 colour and backward pass.
+void launchBlendPixels(const FrameParams& p, cudaStream_t stream);
 void launchGradColor(const FrameParams& p, cudaStream_t stream);
 void launchGradBackward(const FrameParams& p, cudaStream_t stream);
 size_t rasterSmemBytes();

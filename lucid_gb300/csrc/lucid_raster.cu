@@ -420,9 +420,9 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 	const bool alpha_threshold = (opt_flags & LUCID_OPT_ALPHA_THRESHOLD) != 0;
 	if(tid == 0)
 		s.loaded_view = -1;
-	// the FP64 colour and backward raster passes of a differentiable frame run only when its
-	// fragment store overflowed (otherwise the pixel-parallel gradient kernels do the work)
-	if constexpr(MODE == kRasterStats || MODE == kRasterBackward) {
+	// with a fragment store (differentiable frames, pixel-parallel blend) the other modes run
+	// only when the store overflowed; otherwise the pixel-parallel kernels do the work
+	if constexpr(MODE != kRasterStore) {
 		if(p_first.grad_state && *reinterpret_cast<volatile unsigned long long*>(p_first.grad_state) == 0ull)
 			return;
 	}
@@ -751,6 +751,12 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 					if(t < npix && s.px_state[t] == 0 && wbase == 0 && !fits) {
 						// the first pending pixel alone exceeds the capacity
 						raiseError(p.info, LUCID_ERR_PIXEL_FRAGMENTS, uint32_t(bin), uint32_t(p0 + t), uint32_t(total));
+						if constexpr(MODE == kRasterStore) {
+							// the store holds only the fragments written so far
+							const int pl = p0 + t, px = bin_x + (pl & 31), py = bin_y + (pl >> 5);
+							if(s.store_ok && px < p.width && py < p.height)
+								p.grad_px_cnt[size_t(py) * p.width + px] = uint32_t(s.px_done[t]);
+						}
 						s.px_state[t] = 1;
 						s.px_T[t] = 0.0f;
 						s.px_c[t][0] = 1.0f, s.px_c[t][1] = 0.0f, s.px_c[t][2] = 0.0f;
@@ -940,7 +946,9 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 							for(int k = lane; k < wc; k += 32) {
 								uint32_t v = V[wb + k];
 								uint32_t band = (v >> 8) & 7u, eslot = v >> 11;
-								p.grad_tris[dst + k] = entryTri(scratch[size_t(band) * band_cap + eslot]);
+								p.grad_tris[dst + k] = eslot < uint32_t(band_cap)
+														   ? entryTri(scratch[size_t(band) * band_cap + eslot])
+														   : 0xffffffffu;
 							}
 						}
 					}

@@ -1,10 +1,14 @@
-// Pixel-parallel kernels of the differentiable frame (no reference counterpart).
+// Pixel-parallel kernels over the fragment store (no reference counterpart).
 //
-// The differentiable forward runs the raster pass in store mode: every pixel's fragments, in
-// exact blend order (nearest first, ties by primitive id), are written as tri slots to a
-// fragment store. Two kernels then work one thread per pixel, many warps per SM, so that the
+// In store mode the raster pass writes every pixel's fragments, in exact blend order (nearest
+// first, ties by primitive id), as tri slots to a fragment store, and skips shading and
+// blending. These kernels then work one thread per pixel, many warps per SM, so that the
 // per-fragment loads of shading overlap the serial per-pixel blend:
 //
+//  blendPixelsKernel   the plain forward's blend (shading.glsl:272-285, 312): FP32
+//                      out += rgb*a*T; T *= 1-a, stop at T == 0 (or T < 1/128 with the alpha
+//                      threshold), additive variant, background, saturate. Same operations in
+//                      the same order as the raster pass's own blend, so the same image bits.
 //  gradColorKernel     shades the pixel's stored fragments (the raster's shadeFragment, same
 //                      FP32 colour) and accumulates the colour in FP64 with an FP64
 //                      transmittance, stopping where the FP32 transmittance of the image reaches
@@ -29,6 +33,44 @@ __device__ __forceinline__ bool gradStoreComplete(const FrameParams& p) {
 	return *reinterpret_cast<const volatile unsigned long long*>(p.grad_state) == 0ull;
 }
 
+__global__ void __launch_bounds__(kGradTileX * kGradTileY) blendPixelsKernel(FrameParams p) {
+	if(!gradStoreComplete(p))
+		return;
+	const int x = blockIdx.x * kGradTileX + threadIdx.x, y = blockIdx.y * kGradTileY + threadIdx.y;
+	if(x >= p.width || y >= p.height)
+		return;
+	const size_t pix = size_t(y) * p.width + x;
+	const uint32_t off = p.grad_px_off[pix], cnt = p.grad_px_cnt[pix];
+	const bool additive = (p.flags & LUCID_OPT_ADDITIVE_BLENDING) != 0;
+	const bool alpha_threshold = (p.flags & LUCID_OPT_ALPHA_THRESHOLD) != 0;
+	float c0 = 0.0f, c1 = 0.0f, c2 = 0.0f, T = 1.0f;
+	for(uint32_t j = 0; j < cnt; j++) {
+		const uint32_t tri = p.grad_tris[off + j];
+		if(tri >= 2u * uint32_t(p.max_visible_quads))
+			continue; // only after a device error (the frame's lucid_info has it)
+		const float4 c = shadeFragment(p, tri, fragmentDepth(p, tri, x, y), x, y);
+		if(additive) {
+			c0 = c0 + c.x * c.w;
+			c1 = c1 + c.y * c.w;
+			c2 = c2 + c.z * c.w;
+		} else {
+			c0 = c0 + (c.x * c.w) * T;
+			c1 = c1 + (c.y * c.w) * T;
+			c2 = c2 + (c.z * c.w) * T;
+			T = T * (1.0f - c.w);
+			if(T == 0.0f || (alpha_threshold && T < (1.0f / 128.0f)))
+				break;
+		}
+	}
+	const float* bg = p.cfg.background_color;
+	float4 o;
+	o.x = fminf(fmaxf(c0 + T * bg[0], 0.0f), 1.0f);
+	o.y = fminf(fmaxf(c1 + T * bg[1], 0.0f), 1.0f);
+	o.z = fminf(fmaxf(c2 + T * bg[2], 0.0f), 1.0f);
+	o.w = 1.0f;
+	reinterpret_cast<float4*>(p.out_rgba)[pix] = o;
+}
+
 __global__ void __launch_bounds__(kGradTileX * kGradTileY) gradColorKernel(FrameParams p) {
 	if(!gradStoreComplete(p))
 		return;
@@ -41,6 +83,8 @@ __global__ void __launch_bounds__(kGradTileX * kGradTileY) gradColorKernel(Frame
 	float T = 1.0f;
 	for(uint32_t j = 0; j < cnt; j++) {
 		const uint32_t tri = p.grad_tris[off + j];
+		if(tri >= 2u * uint32_t(p.max_visible_quads))
+			continue; // only after a device error (the frame's lucid_info has it)
 		const float4 c = shadeFragment(p, tri, fragmentDepth(p, tri, x, y), x, y);
 		acc[0] += double(c.x * c.w) * T64;
 		acc[1] += double(c.y * c.w) * T64;
@@ -88,6 +132,8 @@ __global__ void __launch_bounds__(kGradTileX * kGradTileY) gradBackwardKernel(Fr
 	float T = 1.0f;
 	for(uint32_t j = 0; j < cnt; j++) {
 		const uint32_t tri = p.grad_tris[off + j];
+		if(tri >= 2u * uint32_t(p.max_visible_quads))
+			continue; // only after a device error (the frame's lucid_info has it)
 		const FragmentShade fs = shadeFragmentFull(p, tri, fragmentDepth(p, tri, x, y), x, y);
 		const float4 c = fs.col;
 		const float a = c.w;
@@ -118,6 +164,12 @@ __global__ void __launch_bounds__(kGradTileX * kGradTileY) gradBackwardKernel(Fr
 		if(T == 0.0f)
 			break;
 	}
+}
+
+void launchBlendPixels(const FrameParams& p, cudaStream_t stream) {
+	const dim3 block(kGradTileX, kGradTileY);
+	const dim3 grid((p.width + kGradTileX - 1) / kGradTileX, (p.height + kGradTileY - 1) / kGradTileY);
+	blendPixelsKernel<<<grid, block, 0, stream>>>(p);
 }
 
 void launchGradColor(const FrameParams& p, cudaStream_t stream) {

@@ -176,6 +176,16 @@ class LucidRenderer:
         return out, counts, prims[..., :max_per_pixel]
 
     # -- info / statistics ------------------------------------------------------------------
+    def autotune(self, frame: FrameInputs, stream=None) -> dict:
+        """Runs lucid_autotune on `frame`; the winner stays in the renderer."""
+        scratch = self.new_image()
+        t = _lib.Tuning()
+        fi = frame.c_struct()
+        check(self.lib.lucid_autotune(self.handle, ctypes.byref(fi), _dptr(scratch), ctypes.byref(t),
+                                      _stream_ptr(stream)), "lucid_autotune")
+        return {k: getattr(t, k) for k in ("pixel_blend", "low_high_threshold", "binning_ctas",
+                                           "num_candidates", "frame_ms", "default_ms")}
+
     def render_batch(self, frames, outs=None, stream=None):
         """Renders every (frame, width, height) of `frames` with lucid_render_batch; returns the
         output images (allocated unless `outs` is given)."""

@@ -117,3 +117,31 @@ def test_info_struct_layout():
     assert _lib.Info.error_code.offset == 1152 * 4
     assert ctypes.sizeof(_lib.Info) == 1216 * 4
     assert ctypes.sizeof(scenes.LucidConfig) == 352
+
+
+def test_struct_sizes_match_header(tmp_path):
+    """sizeof / offsetof of the public structs, compiled from include/lucid_gb300.h with the host
+    C compiler, equal the ctypes mirrors."""
+    import shutil
+    import subprocess
+    from lucid_gb300 import _lib
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    src = tmp_path / "sizes.c"
+    src.write_text(
+        '#include <stdio.h>\n#include <stddef.h>\n#include "lucid_gb300.h"\n'
+        "int main(void) {\n"
+        ' printf("%zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(lucid_options), sizeof(lucid_frame_inputs),'
+        " sizeof(lucid_view), sizeof(lucid_tuning), sizeof(lucid_info), sizeof(lucid_camera),"
+        " offsetof(lucid_options, grad_store_fragments), offsetof(lucid_view, out_rgba));\n"
+        " return 0;\n}\n")
+    exe = tmp_path / "sizes"
+    subprocess.run([cc, "-I", os.path.join(root, "include"), str(src), "-o", str(exe)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], check=True, capture_output=True,
+                                          text=True).stdout.split()]
+    want = [ctypes.sizeof(_lib.Options), ctypes.sizeof(_lib.FrameInputsC), ctypes.sizeof(_lib.ViewC),
+            ctypes.sizeof(_lib.Tuning), ctypes.sizeof(_lib.Info), ctypes.sizeof(_lib.CameraC),
+            _lib.Options.grad_store_fragments.offset, _lib.ViewC.out_rgba.offset]
+    assert got == want

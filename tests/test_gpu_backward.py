@@ -104,8 +104,9 @@ def test_backward_without_fragment_store(gpu, oracle, store):
     a = gpu_grads(sc, target)
     b = gpu_grads(sc, target, grad_store_fragments=store)
     np.testing.assert_array_equal(a["image"], b["image"])
-    assert rel_err(b["dvc"].ravel(), a["dvc"].ravel()).max() <= 1e-5
-    assert rel_err(b["dop"], a["dop"]).max() <= 1e-5
+    # same arithmetic per fragment; the FP32 atomic sums differ in order
+    assert rel_err(b["dvc"].ravel(), a["dvc"].ravel()).max() <= TOL
+    assert rel_err(b["dop"], a["dop"]).max() <= TOL
 
 
 def test_backward_rejects_unsupported(gpu):
