@@ -48,6 +48,8 @@ def parse_args():
     ap.add_argument("--impl", default="lucid_gb300", choices=["lucid_gb300", "reference"])
     ap.add_argument("--cpu-sample-bins", type=int, default=0, help="bins in the CPU sample (0 = auto)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the forward+backward and batched-view measurements (profiling runs)")
     ap.add_argument("--workload", default=WORKLOAD,
                     help="scenes.workload name (the default is the benchmark workload; smaller "
                          "ones exist for profiler captures)")
@@ -340,11 +342,11 @@ def main():
         lucid_build.build()
     if dist is not None:
         dist.barrier()
-    from lucid_gb300 import scenes, _lib
+    from lucid_gb300 import replicas, scenes, _lib
     from lucid_gb300.renderer import FrameInputs, LucidRenderer
 
     # replicas: each rank renders its own seeded frame of the same workload
-    scene = scenes.workload(args.workload, seed=1 + rank)
+    scene = scenes.workload(args.workload, seed=replicas.rank_seed(1, rank))
     r = LucidRenderer(scene.width, scene.height, max_input_quads=scene.num_quads,
                       max_visible_quads=scene.num_quads, max_bin_refs=8 * scene.num_quads)
     frame = FrameInputs.from_scene(scene)
@@ -386,13 +388,9 @@ def main():
             dist.barrier()
         torch.cuda.synchronize()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    total_ms = float(sum(step_ms))
-    if dist is not None:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    # replicas: every rank's fragments over the slowest rank's time
+    value, total_ms, _ = replicas.aggregate(float(sum(step_ms)), fragments * args.steps, dist, "cuda")
     ms_per_step = total_ms / args.steps
-    value = fragments * args.steps * world / (total_ms / 1e3)
 
     # ---- raster kernel alone (roofline): pass-level API, events around lucid_raster
     r.quad_setup(frame)
@@ -437,12 +435,13 @@ def main():
         host_out.copy_(out, non_blocking=True)
     e1.record(stream)
     torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1) / args.steps
-    e2e_value = fragments * world / (e2e_ms / 1e3)
+    e2e_value, e2e_total_ms, _ = replicas.aggregate(e0.elapsed_time(e1), fragments * args.steps, dist, "cuda")
+    e2e_ms = e2e_total_ms / args.steps
 
     # ---- forward+backward workload (rank 0 only)
-    fwd_bwd = grad_bench(max(5, args.steps), max(3, args.warmup), flush_buf) if rank == 0 else None
-    batch = batch_bench(max(5, args.steps), max(3, args.warmup), flush_buf) if rank == 0 else None
+    extras = rank == 0 and not args.no_extras
+    fwd_bwd = grad_bench(max(5, args.steps), max(3, args.warmup), flush_buf) if extras else None
+    batch = batch_bench(max(5, args.steps), max(3, args.warmup), flush_buf) if extras else None
 
     # ---- CPU baseline (rank 0, N=1 only)
     cpu = None
@@ -477,7 +476,7 @@ def main():
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
             "gpu_launches": KERNELS_PER_FRAME * args.steps,
-            "mtri_per_s": scene.num_tris * args.steps * world / (total_ms / 1e3) / 1e6,
+            "mtri_per_s": scene.num_tris * args.steps * world / (total_ms / 1e3) / 1e6,  # equal tris per rank
             "fwd_bwd": fwd_bwd,
             "batch": batch,
         }
