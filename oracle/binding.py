@@ -70,7 +70,7 @@ def _ptr(a):
 
 def run(scene, max_visible_quads: int | None = None, raster: bool = True, image64: bool = False,
         bin_subset=None, threads: int = 1, max_per_pixel: int = 0, flags: int = 0,
-        low_high_threshold: int = 1024, setup_outputs: bool = True):
+        low_high_threshold: int = 1024, setup_outputs: bool = True, order_mode: int = 0):
     """Runs the oracle on a ``lucid_gb300.scenes.Scene``; returns a dict of numpy arrays."""
     L = lib()
     mvq = max_visible_quads or max(1024, scene.num_quads)
@@ -110,7 +110,7 @@ def run(scene, max_visible_quads: int | None = None, raster: bool = True, image6
     cfg = scene.config
     ins = OracleInputs(
         width=w, height=h, max_visible_quads=mvq, low_high_threshold=low_high_threshold,
-        flags=flags, order_mode=0, positions=_ptr(positions), colors=_ptr(colors),
+        flags=flags, order_mode=order_mode, positions=_ptr(positions), colors=_ptr(colors),
         color_format=scene.color_format, num_verts=positions.shape[0], quads_ib=_ptr(quads),
         num_quads=quads.shape[0], num_instances=inst.shape[0], instances=_ptr(inst),
         instance_colors=_ptr(icol), tri_opacity=_ptr(opac), config=ctypes.addressof(cfg),
@@ -136,7 +136,8 @@ def run(scene, max_visible_quads: int | None = None, raster: bool = True, image6
         bin_count=outs.bin_count, bin_count_x=outs.bin_count_x, bin_count_y=outs.bin_count_y,
         bin_level_counts=tuple(outs.bin_level_counts), num_fragments=int(outs.num_fragments),
         num_hblock_tris=int(outs.num_hblock_tris),
-        max_pixel_fragments=int(outs.max_pixel_fragments), max_visible_quads=mvq)
+        max_pixel_fragments=int(outs.max_pixel_fragments), invalid_pixels=int(outs.invalid_pixels),
+        max_visible_quads=mvq)
     return out
 
 

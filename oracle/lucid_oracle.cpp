@@ -800,6 +800,497 @@ void rasterBin(const State& s, int bin, oracle_outputs* out, std::vector<std::ve
 	}
 }
 
+// ---------------------------------------------------------------------------------------------
+// Reference-order mode (order_mode 1): the reference's own per-pixel order and blend.
+//
+// LOW bins (raster_low.glsl): per 8x8 block, the tris whose row spans (scan started at the tri's
+// first 8-row block row, generateRowTris :39-64) touch the block get a 22-bit key at their
+// coverage centroid in the block (generateBlocks :101-131; rasterHalfBlockCentroid and
+// rasterBlockDepth, raster.glsl:142-176) and are sorted when the block holds more than
+// RC_COLOR_SIZE tris (:144-150). A block of more than 256 tris promotes the bin to the HIGH path
+// (:93-103, :211-219).
+// HIGH bins (raster_high.glsl): per 8x4 half-block (scan started at the tri's first half-block
+// row, :60-81), an 18-bit key at the centroid (:168-186), always sorted; more than 16384 tris in
+// a half-block row, or more than 4096 in one half-block by the range estimate of
+// computeRBlockGroups (:114-147), paint the bin red (1, 0, 0, 0) (:297-301).
+// Equal keys, which the reference leaves in shared-memory arrival order (not deterministic),
+// are ordered by input primitive id; blocks of <= 3 tris (unsorted in the reference) are in
+// primitive-id order.
+// A pixel's samples are its block's sorted tris that cover it, shaded with the scene lighting
+// and encoded RGBA8 (shadeSample, shading.glsl:107-184), then reduced through the 3-deep depth
+// window (reduceSample / finishReduceSamples, shading.glsl:229-314); the accumulated colour is
+// saturated at the end of every 256-fragment segment of the half-block (shadeAndReduceSamples,
+// raster.glsl:361-398). The alpha-threshold variant (a subgroup vote in the reference) is not
+// part of this mode.
+
+// x^y for finite x > 0 as exp2(y * log2(x)): log2 of the mantissa m in [sqrt(1/2), sqrt(2)) from
+// the series 2 atanh(t) = ln(m), t = (m - 1) / (m + 1), up to t^13; 2^f, f in [0, 1), from the
+// Taylor series of e^(f ln 2) up to degree 10. The CUDA path evaluates the same float
+// operations in the same order (no FMA on either side), so both round identically.
+float refPow(float x, float y) {
+	if(x != x)
+		return x;
+	if(x <= 0.0f)
+		return x == 0.0f ? 0.0f : NAN;
+	if(x == INFINITY)
+		return y > 0.0f ? INFINITY : 0.0f;
+	int e = 0;
+	uint32_t b = fbits(x);
+	if(((b >> 23) & 0xffu) == 0u) { // subnormal
+		x = x * 8388608.0f;
+		b = fbits(x);
+		e = -23;
+	}
+	e += int((b >> 23) & 0xffu) - 127;
+	float m = bitsf((b & 0x7fffffu) | 0x3f800000u);
+	if(m > 0x1.6a09e6p+0f) {
+		m = m * 0.5f;
+		e = e + 1;
+	}
+	const float t = (m - 1.0f) / (m + 1.0f);
+	const float t2 = t * t;
+	float sr = 0x1.3b13b2p-4f;      // 1/13
+	sr = sr * t2 + 0x1.745d18p-4f; // 1/11
+	sr = sr * t2 + 0x1.c71c72p-4f; // 1/9
+	sr = sr * t2 + 0x1.24924ap-3f; // 1/7
+	sr = sr * t2 + 0x1.99999ap-3f; // 1/5
+	sr = sr * t2 + 0x1.555556p-2f; // 1/3
+	sr = sr * t2 + 1.0f;
+	const float ln_m = (2.0f * t) * sr;
+	const float l2 = float(e) + ln_m * 0x1.715476p+0f; // 1/ln 2
+	const float z = y * l2;
+	if(z >= 128.0f)
+		return INFINITY;
+	if(z < -149.0f)
+		return 0.0f;
+	const float k = floorf(z);
+	const float u = (z - k) * 0x1.62e43p-1f; // ln 2
+	float pe = 0x1.27e4fcp-22f;    // 1/10!
+	pe = pe * u + 0x1.71de3ap-19f; // 1/9!
+	pe = pe * u + 0x1.a01a02p-16f; // 1/8!
+	pe = pe * u + 0x1.a01a02p-13f; // 1/7!
+	pe = pe * u + 0x1.6c16c2p-10f; // 1/6!
+	pe = pe * u + 0x1.111112p-7f;  // 1/5!
+	pe = pe * u + 0x1.555556p-5f;  // 1/4!
+	pe = pe * u + 0x1.555556p-3f;  // 1/3!
+	pe = pe * u + 0.5f;
+	pe = pe * u + 1.0f;
+	pe = pe * u + 1.0f;
+	int ki = int(k);
+	if(ki < -126) { // scale in two steps to stay within normal exponents
+		pe = pe * bitsf(uint32_t(ki + 126 + 127) << 23);
+		ki = -126;
+	}
+	return pe * bitsf(uint32_t(ki + 127) << 23);
+}
+
+// funcs.glsl:61-66
+inline V3 decodeNormalUint(uint32_t n) {
+	const float s = 0x1.00804p-9f; // 1/511
+	return v3((float((n >> 0) & 0x3ffu) - 512.0f) * s, (float((n >> 10) & 0x3ffu) - 512.0f) * s,
+			  (float((n >> 20) & 0x3ffu) - 512.0f) * s);
+}
+
+// funcs.glsl:118-121
+inline uint32_t encodeRGBA8(const float c[4]) {
+	return f2u(c[0] * 255.0f) | (f2u(c[1] * 255.0f) << 8) | (f2u(c[2] * 255.0f) << 16) |
+		   (f2u(c[3] * 255.0f) << 24);
+}
+
+inline float saturate(float v) { return fminf(fmaxf(v, 0.0f), 1.0f); }
+
+// shadeSample (shading.glsl:107-184): colour as the exact mode's shading, then the flat tri
+// normal, sun light and finalShading (funcs.glsl:153-164, 261-271), RGBA8; 0 when alpha is 0.
+uint32_t shadeRef(const State& s, uint32_t tri, uint32_t prim, int px, int py, float& depth) {
+	const uint32_t* d = &s.tri_depth[size_t(tri) * 4];
+	const float inv_ray_pos = bitsf(d[0]) * float(px) + (bitsf(d[1]) * float(py) + bitsf(d[2]));
+	depth = inv_ray_pos;
+	float c[4];
+	shadeFragment(s, Frag{0u, prim, tri, inv_ray_pos}, px, py, c);
+	if(c[3] == 0.0f)
+		return 0u;
+	const lucid_lighting& L = s.in->config->lighting;
+	const V3 n = decodeNormalUint(s.tri_normals[tri]);
+	const float dn = (-L.sun_dir[0]) * n.x + (-L.sun_dir[1]) * n.y + (-L.sun_dir[2]) * n.z;
+	const float light = fmaxf(0.0f, dn * 0x1.666666p-1f + 0x1.333334p-2f); // * 0.7 + 0.3
+	for(int ch = 0; ch < 3; ch++) {
+		const float cv = c[ch];
+		const float lin = cv < 0x1.4b5dccp-5f ? 0x1.3d0722p-4f * cv // 0.04045, 1/12.92
+											  : refPow((cv + 0x1.c28f5cp-5f) * 0x1.e54edep-1f, 0x1.333334p+1f);
+		const float amb = L.ambient_color[ch] * L.ambient_power;
+		const float dif = (L.sun_color[ch] * L.sun_power) * light;
+		const float v = lin * (amb + dif);
+		const float sr = v < 0x1.9a5c38p-9f ? 0x1.9d70a4p+3f * v // 0.0031308, 12.92
+											: 0x1.0e147ap+0f * refPow(v, 0x1.aaaaaap-2f) - 0x1.c28f5cp-5f;
+		c[ch] = saturate(sr);
+	}
+	return encodeRGBA8(c);
+}
+
+// ReductionContext (shading.glsl:196-227); depth slots 4 with LUCID_OPT_VISUALIZE_ERRORS
+struct RefReduce {
+	float depth[4];
+	uint32_t col[3];
+	float trans;
+	float out[3];
+	int depth_size;
+	bool additive, invalid;
+
+	void init(int dsize, bool add) {
+		for(float& v : depth)
+			v = 999999999.0f;
+		col[0] = col[1] = col[2] = 0u;
+		trans = 1.0f;
+		out[0] = out[1] = out[2] = 0.0f;
+		depth_size = dsize;
+		additive = add;
+		invalid = false;
+	}
+	void swapSlots(int a, int b) {
+		std::swap(depth[a], depth[b]);
+		if(a < 3 && b < 3)
+			std::swap(col[a], col[b]);
+	}
+	void blend(uint32_t c) {
+		float cur[4];
+		decodeRGBA8(c, cur);
+		if(additive) {
+			for(int ch = 0; ch < 3; ch++)
+				out[ch] = out[ch] + cur[ch] * cur[3];
+		} else {
+			for(int ch = 0; ch < 3; ch++)
+				out[ch] = out[ch] + (cur[ch] * cur[3]) * trans;
+			trans = trans * (1.0f - cur[3]);
+		}
+	}
+	// reduceSample (shading.glsl:229-294) for one sample
+	void sample(uint32_t color, float dep) {
+		if(dep > depth[0]) {
+			std::swap(color, col[0]);
+			std::swap(dep, depth[0]);
+			if(depth[0] > depth[1]) {
+				swapSlots(0, 1);
+				if(depth[1] > depth[2]) {
+					swapSlots(1, 2);
+					int i = 3;
+					for(; i < depth_size && depth[i - 1] > depth[i]; i++)
+						swapSlots(i - 1, i);
+					if(depth_size == 4 && i == depth_size) {
+						invalid = true;
+						out[0] = 1.0f, out[1] = 0.0f, out[2] = 0.0f;
+						trans = 0.0f;
+						return;
+					}
+				}
+			}
+		}
+		for(int i = depth_size - 1; i > 0; i--)
+			depth[i] = depth[i - 1];
+		depth[0] = dep;
+		if(col[2] != 0u)
+			blend(col[2]);
+		col[2] = col[1], col[1] = col[0], col[0] = color;
+	}
+	void endSegment() {
+		for(float& v : out)
+			v = saturate(v);
+	}
+	// finishReduceSamples (shading.glsl:296-314)
+	void finish(const float* bg, float rgba[4]) {
+		for(int i = 2; i >= 0; i--)
+			if(col[i] != 0u)
+				blend(col[i]);
+		for(int ch = 0; ch < 3; ch++)
+			rgba[ch] = saturate(out[ch] + trans * bg[ch]);
+		rgba[3] = 1.0f;
+	}
+};
+
+struct RefTri {
+	uint32_t tri, prim;
+	RowSpan rows[32];
+};
+
+struct RefEntry {
+	uint32_t key, prim;
+	int t; // index into the bin's RefTri list
+};
+
+// Per-row spans of one tri inside one bin with the scan started at the tri's first row group
+// of `group` rows (8: raster_low generateRowTris, 4: raster_high generateRowTris).
+void triBinRowsFrom(const uint32_t* sc, int bin_x, int bin_y, int group, RowSpan rows[32]) {
+	for(int r = 0; r < 32; r++)
+		rows[r] = RowSpan{31, 0};
+	const int shift = group == 8 ? 3 : 2;
+	int ymin = int(sc[3] & 0xffffu) - bin_y, ymax = int(sc[3] >> 16) - bin_y;
+	int min_g = std::min(std::max(ymin, 0), 31) >> shift;
+	int max_g = std::min(std::max(ymax, 0), 31) >> shift;
+	float sx = float(bin_x), sy = float(bin_y + min_g * group);
+	float mn[3], mx[3], step[3];
+	uint32_t sg = sc[7];
+	for(int i = 0; i < 3; i++) {
+		step[i] = bitsf(sc[4 + i]);
+		float scan = bitsf(sc[i]) + (step[i] * sy - sx);
+		bool xneg = (sg >> i) & 1u;
+		mn[i] = xneg ? -INFINITY : scan;
+		mx[i] = xneg ? scan : INFINITY;
+	}
+	for(int row = min_g * group; row < max_g * group + group; row++) {
+		float fl = fmaxf(fmaxf(mn[0], mn[1]), fmaxf(mn[2], 0.0f));
+		float fh = fminf(fminf(mx[0], mx[1]), fminf(mx[2], float(kBinSize)));
+		int lo = f2i(fminf(fl, 33.0f));
+		int hi = f2i(fmaxf(fh, -1.0f)) - 1;
+		if(lo > hi)
+			lo = 31, hi = 0;
+		for(int i = 0; i < 3; i++)
+			mn[i] += step[i], mx[i] += step[i];
+		rows[row] = RowSpan{lo, hi};
+	}
+}
+
+// 4-bit mask of the 8-pixel columns touched by rows [r0, r0 + 4) (BX_MASK_ROW, raster.glsl:123-127)
+inline uint32_t rowGroupColumns(const RowSpan* rows, int r0) {
+	uint32_t m = 0;
+	for(int r = r0; r < r0 + 4; r++)
+		if(rows[r].lo <= rows[r].hi)
+			m |= ((0xfu << (rows[r].lo >> 3)) & (0xfu >> (3 - (rows[r].hi >> 3))));
+	return m;
+}
+
+// rasterHalfBlockCentroid (raster.glsl:142-150) over rows [r0, r0 + 4) from column startx
+inline void halfBlockCentroid(const RowSpan* rows, int r0, int startx, float& cx, float& cy, int& nfrag) {
+	const float wy[4] = {1.0f, 3.0f, 5.0f, 7.0f};
+	float px[4], py[4];
+	nfrag = 0;
+	for(int k = 0; k < 4; k++) {
+		int xmin = std::max(rows[r0 + k].lo - startx, 0);
+		int xmax = std::min(rows[r0 + k].hi - startx, 7);
+		int count = std::max(xmax - xmin + 1, 0);
+		px[k] = float(xmin * 2 + count) * float(count);
+		py[k] = wy[k] * float(count);
+		nfrag += count;
+	}
+	cx = px[0] + px[1] + px[2] + px[3];
+	cy = py[0] + py[1] + py[2] + py[3];
+}
+
+// rasterBlockDepth (raster.glsl:170-176); inversesqrt = 1 / sqrt
+inline uint32_t refBlockKey(const State& s, uint32_t tri, float cx, float cy, int nfrag, float bx, float by,
+							float range) {
+	const uint32_t* d = &s.tri_depth[size_t(tri) * 4];
+	const float scale = 0.5f / float(nfrag);
+	const float px = cx * scale + bx, py = cy * scale + by;
+	const float ray_pos = bitsf(d[0]) * px + (bitsf(d[1]) * py + bitsf(d[2]));
+	const float isq = 1.0f / sqrtf(ray_pos + 1.0f);
+	return f2u(range * saturate(isq));
+}
+
+inline bool refLess(const RefEntry& a, const RefEntry& b) {
+	return a.key != b.key ? a.key < b.key : a.prim < b.prim;
+}
+
+// Reduces the samples of every pixel of one half-block (8 x 4 pixels at local (hx*8, hy*4))
+// from a list of tris in blend order; segments of 256 fragments in list order, pixels of a tri
+// in row-major order (unpackSamples, raster.glsl:299-357).
+void refReduceHalfBlock(const State& s, int bin_x, int bin_y, int hx, int hy, const std::vector<RefTri>& tris,
+						const std::vector<RefEntry>& list, oracle_outputs* out, uint64_t& nfrag, uint64_t& ninvalid) {
+	const oracle_inputs* in = s.in;
+	const bool additive = (in->flags & LUCID_OPT_ADDITIVE_BLENDING) != 0;
+	const bool visualize = (in->flags & LUCID_OPT_VISUALIZE_ERRORS) != 0;
+	RefReduce ctx[32];
+	int last_seg[32], nsamp[32];
+	for(int i = 0; i < 32; i++) {
+		ctx[i].init(visualize ? 4 : 3, additive);
+		last_seg[i] = -1;
+		nsamp[i] = 0;
+	}
+	const int startx = hx * 8, r0 = hy * 4;
+	uint32_t offset = 0;
+	for(const RefEntry& e : list) {
+		const RefTri& t = tris[size_t(e.t)];
+		uint32_t rank = 0;
+		for(int k = 0; k < 4; k++) {
+			const RowSpan sp = t.rows[r0 + k];
+			int xmin = std::max(sp.lo - startx, 0), xmax = std::min(sp.hi - startx, 7);
+			for(int x = xmin; x <= xmax; x++, rank++) {
+				const int pl = k * 8 + x;
+				const int seg = int((offset + rank) >> 8);
+				if(last_seg[pl] >= 0 && seg != last_seg[pl])
+					ctx[pl].endSegment();
+				last_seg[pl] = seg;
+				const int pxx = bin_x + startx + x, py = bin_y + r0 + k;
+				float dep;
+				const uint32_t color = shadeRef(s, t.tri, t.prim, pxx, py, dep);
+				ctx[pl].sample(color, dep);
+				if(pxx < s.w && py < s.h && out->frag_prims) {
+					const size_t pix = size_t(py) * s.w + pxx;
+					if(nsamp[pl] < out->max_per_pixel)
+						out->frag_prims[pix * out->max_per_pixel + nsamp[pl]] = int32_t(t.prim);
+				}
+				nsamp[pl]++;
+			}
+		}
+		offset += rank;
+	}
+	nfrag += offset;
+	const float* bg = in->config->background_color;
+	for(int pl = 0; pl < 32; pl++) {
+		const int pxx = bin_x + startx + (pl & 7), py = bin_y + r0 + (pl >> 3);
+		if(last_seg[pl] >= 0)
+			ctx[pl].endSegment();
+		if(pxx >= s.w || py >= s.h)
+			continue;
+		const size_t pix = size_t(py) * s.w + pxx;
+		float rgba[4];
+		ctx[pl].finish(bg, rgba);
+		if(ctx[pl].invalid)
+			ninvalid++;
+		if(out->image)
+			for(int ch = 0; ch < 4; ch++)
+				out->image[pix * 4 + ch] = rgba[ch];
+		if(out->frag_counts)
+			out->frag_counts[pix] = nsamp[pl];
+	}
+}
+
+void rasterBinRef(const State& s, int bin, oracle_outputs* out, uint64_t& nfrag, uint64_t& nhbt,
+				  uint32_t& maxfrag, uint64_t& ninvalid) {
+	const oracle_inputs* in = s.in;
+	const int bx = bin % s.bcx, by = bin / s.bcx;
+	const int bin_x = bx * kBinSize, bin_y = by * kBinSize;
+	std::vector<std::pair<uint32_t, uint32_t>> tri_ids; // (tri slot, primitive id)
+	for(uint32_t e : s.bin_quads[bin]) {
+		const uint32_t quad = e & 0x0fffffffu;
+		for(int second = 0; second < 2; second++)
+			if(!((e >> (30 + second)) & 1u))
+				tri_ids.push_back({quad * 2 + second, s.quad_source[quad] * 2 + second});
+	}
+	for(uint32_t t : s.bin_tris[bin])
+		tri_ids.push_back({t, s.quad_source[t >> 1] * 2 + (t & 1)});
+	const int64_t num_tris = int64_t(s.bin_tris[bin].size()) + 2 * int64_t(s.bin_quads[bin].size());
+	std::vector<RefTri> tris(tri_ids.size());
+	std::vector<std::vector<RefEntry>> lists;
+	auto writeBackground = [&](const float* rgba4) {
+		for(int r = 0; r < 32; r++)
+			for(int x = 0; x < 32; x++) {
+				const int pxx = bin_x + x, py = bin_y + r;
+				if(pxx >= s.w || py >= s.h)
+					continue;
+				const size_t pix = size_t(py) * s.w + pxx;
+				if(out->image)
+					for(int ch = 0; ch < 4; ch++)
+						out->image[pix * 4 + ch] = rgba4[ch];
+				if(out->frag_counts)
+					out->frag_counts[pix] = 0;
+			}
+	};
+	if(num_tris == 0) { // EMPTY bins are not rastered; the image keeps the background
+		const float* bg = in->config->background_color;
+		const float rgba[4] = {saturate(bg[0]), saturate(bg[1]), saturate(bg[2]), 1.0f};
+		writeBackground(rgba);
+		return;
+	}
+	bool high = num_tris >= in->low_high_threshold;
+	if(!high) {
+		// raster_low: 8x8 blocks
+		for(size_t i = 0; i < tris.size(); i++) {
+			tris[i].tri = tri_ids[i].first, tris[i].prim = tri_ids[i].second;
+			triBinRowsFrom(&s.tri_scan[size_t(tris[i].tri) * 8], bin_x, bin_y, 8, tris[i].rows);
+		}
+		lists.assign(16, {});
+		for(size_t i = 0; i < tris.size(); i++)
+			for(int brow = 0; brow < 4; brow++) {
+				const uint32_t m = rowGroupColumns(tris[i].rows, brow * 8) | rowGroupColumns(tris[i].rows, brow * 8 + 4);
+				for(int bcol = 0; bcol < 4; bcol++)
+					if((m >> bcol) & 1u)
+						lists[size_t(brow * 4 + bcol)].push_back(RefEntry{0u, tris[i].prim, int(i)});
+			}
+		for(auto& l : lists)
+			if(l.size() > 256)
+				high = true; // promoted (raster_low.glsl:211-219)
+		if(!high) {
+			for(int blk = 0; blk < 16; blk++) {
+				const int brow = blk >> 2, bcol = blk & 3;
+				auto& l = lists[size_t(blk)];
+				for(RefEntry& e : l) {
+					const RefTri& t = tris[size_t(e.t)];
+					float cx0, cy0, cx1, cy1;
+					int n0, n1;
+					halfBlockCentroid(t.rows, brow * 8, bcol * 8, cx0, cy0, n0);
+					halfBlockCentroid(t.rows, brow * 8 + 4, bcol * 8, cx1, cy1, n1);
+					e.key = n0 + n1 > 0 ? refBlockKey(s, t.tri, cx0 + cx1, cy0 + cy1, n0 + n1, float(bin_x + bcol * 8),
+													  float(bin_y + brow * 8), float(0x3ffffe))
+										: 0u;
+				}
+				if(l.size() > 3)
+					std::sort(l.begin(), l.end(), refLess);
+				else
+					std::sort(l.begin(), l.end(), [](const RefEntry& a, const RefEntry& b) { return a.prim < b.prim; });
+				nhbt += 2 * l.size();
+				refReduceHalfBlock(s, bin_x, bin_y, bcol, brow * 2, tris, l, out, nfrag, ninvalid);
+				refReduceHalfBlock(s, bin_x, bin_y, bcol, brow * 2 + 1, tris, l, out, nfrag, ninvalid);
+			}
+		}
+	}
+	if(high) {
+		// raster_high: 8x4 half-blocks, scan started at the half-block row
+		for(size_t i = 0; i < tris.size(); i++) {
+			tris[i].tri = tri_ids[i].first, tris[i].prim = tri_ids[i].second;
+			triBinRowsFrom(&s.tri_scan[size_t(tris[i].tri) * 8], bin_x, bin_y, 4, tris[i].rows);
+		}
+		lists.assign(32, {});
+		int row_count[8] = {0, 0, 0, 0, 0, 0, 0, 0}, estimate[32];
+		for(int& v : estimate)
+			v = 0;
+		for(size_t i = 0; i < tris.size(); i++)
+			for(int hrow = 0; hrow < 8; hrow++) {
+				const uint32_t m = rowGroupColumns(tris[i].rows, hrow * 4);
+				if(m == 0)
+					continue;
+				row_count[hrow]++;
+				const int lo = __builtin_ctz(m), hi = 31 - __builtin_clz(m);
+				for(int c = lo; c <= hi; c++)
+					estimate[hrow * 4 + c]++;
+				for(int c = 0; c < 4; c++)
+					if((m >> c) & 1u)
+						lists[size_t(hrow * 4 + c)].push_back(RefEntry{0u, tris[i].prim, int(i)});
+			}
+		bool error = false;
+		for(int r = 0; r < 8; r++)
+			error |= row_count[r] > 16384;
+		for(int v : estimate)
+			error |= v > 4096;
+		if(error) {
+			const float red[4] = {1.0f, 0.0f, 0.0f, 0.0f};
+			writeBackground(red);
+			return;
+		}
+		for(int hb = 0; hb < 32; hb++) {
+			const int hrow = hb >> 2, hcol = hb & 3;
+			auto& l = lists[size_t(hb)];
+			for(RefEntry& e : l) {
+				const RefTri& t = tris[size_t(e.t)];
+				float cx, cy;
+				int n;
+				halfBlockCentroid(t.rows, hrow * 4, hcol * 8, cx, cy, n);
+				e.key = n > 0 ? refBlockKey(s, t.tri, cx, cy, n, float(bin_x + hcol * 8), float(bin_y + hrow * 4),
+											float(0x7fffe))
+							  : 0u;
+			}
+			std::sort(l.begin(), l.end(), refLess);
+			nhbt += l.size();
+			refReduceHalfBlock(s, bin_x, bin_y, hcol, hrow, tris, l, out, nfrag, ninvalid);
+		}
+	}
+	if(out->frag_counts)
+		for(int r = 0; r < 32; r++)
+			for(int x = 0; x < 32; x++) {
+				const int pxx = bin_x + x, py = bin_y + r;
+				if(pxx < s.w && py < s.h)
+					maxfrag = std::max(maxfrag, uint32_t(out->frag_counts[size_t(py) * s.w + pxx]));
+			}
+}
+
 void raster(State& s, oracle_outputs* out) {
 	const oracle_inputs* in = s.in;
 	std::vector<int> bins;
@@ -813,7 +1304,7 @@ void raster(State& s, oracle_outputs* out) {
 	}
 	int nt = std::max(1, in->num_threads);
 	std::atomic<size_t> next{0};
-	std::vector<uint64_t> nf(nt, 0), nh(nt, 0);
+	std::vector<uint64_t> nf(nt, 0), nh(nt, 0), ni(nt, 0);
 	std::vector<uint32_t> mf(nt, 0);
 	auto worker = [&](int tid) {
 		std::vector<std::vector<Frag>> px(1024);
@@ -821,7 +1312,10 @@ void raster(State& s, oracle_outputs* out) {
 			size_t i = next.fetch_add(1);
 			if(i >= bins.size())
 				break;
-			rasterBin(s, bins[i], out, px, nf[tid], nh[tid], mf[tid]);
+			if(in->order_mode == 1)
+				rasterBinRef(s, bins[i], out, nf[tid], nh[tid], mf[tid], ni[tid]);
+			else
+				rasterBin(s, bins[i], out, px, nf[tid], nh[tid], mf[tid]);
 		}
 	};
 	if(nt == 1)
@@ -833,8 +1327,9 @@ void raster(State& s, oracle_outputs* out) {
 		for(auto& t : th)
 			t.join();
 	}
-	out->num_fragments = 0, out->num_hblock_tris = 0, out->max_pixel_fragments = 0;
+	out->num_fragments = 0, out->num_hblock_tris = 0, out->max_pixel_fragments = 0, out->invalid_pixels = 0;
 	for(int t = 0; t < nt; t++) {
+		out->invalid_pixels += ni[t];
 		out->num_fragments += nf[t];
 		out->num_hblock_tris += nh[t];
 		out->max_pixel_fragments = std::max(out->max_pixel_fragments, mf[t]);
@@ -1107,8 +1602,10 @@ extern "C" double oracle_grad_fd(void* ctx, const double* vc, const double* op, 
 
 extern "C" int oracle_run(const oracle_inputs* in, oracle_outputs* out) {
 	if(!in || !out || !in->config || in->width <= 0 || in->height <= 0 ||
-	   in->max_visible_quads <= 0 || in->order_mode != 0)
+	   in->max_visible_quads <= 0 || in->order_mode < 0 || in->order_mode > 1)
 		return 1;
+	if(in->order_mode == 1 && (in->flags & LUCID_OPT_ALPHA_THRESHOLD))
+		return 1; // a subgroup vote in the reference; not part of the reference-order mode
 	if(in->num_quads > 0 && (!in->positions || !in->quads_ib || !in->instances))
 		return 1;
 	State s;

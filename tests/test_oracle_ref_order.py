@@ -1,0 +1,82 @@
+"""The oracle's reference-order mode (order_mode 1) against an independent float32 Python model
+of the reference GLSL (tests/ref_order_model.py): per-pixel sample order, image bits and the
+invalid-pixel count, on LOW bins, HIGH bins (a low LOW/HIGH threshold) and with the depth-4
+error window; plus properties of the mode."""
+import math
+
+import numpy as np
+import pytest
+
+from lucid_gb300 import scenes
+from tests.ref_order_model import Model, pow_series
+
+VISUALIZE_ERRORS = 8
+
+
+def _check(sc, flags, threshold, oracle):
+    out = oracle.run(sc, order_mode=1, max_per_pixel=256, flags=flags, low_high_threshold=threshold)
+    img, order, invalid = Model(sc, out, flags=flags).render(low_high_threshold=threshold)
+    np.testing.assert_array_equal(out["image"], img)
+    for (py, px), prims in order.items():
+        n = min(len(prims), 256)
+        assert out["frag_counts"][py, px] == len(prims)
+        assert [int(v) for v in out["frag_prims"][py, px, :n]] == prims[:n], (py, px)
+    assert out["invalid_pixels"] == invalid
+    return out
+
+
+@pytest.mark.parametrize("case", ["low", "low_fp32_opacity_errors", "high", "high_additive"])
+def test_ref_order_matches_model(oracle, case):
+    if case == "low":
+        sc = scenes.small_scene(64, 48, 160, seed=3, area_median=150.0)
+        out = _check(sc, 0, 1024, oracle)
+        assert out["bin_level_counts"][2] > 0
+    elif case == "low_fp32_opacity_errors":
+        sc = scenes.random_tris(48, 32, 160, seed=4, color_format=scenes.COLOR_RGBA32F,
+                                tri_opacity_range=(0.1, 0.9), area_median=150.0,
+                                background=(0.2, 0.3, 0.4, 1.0))
+        out = _check(sc, VISUALIZE_ERRORS, 1024, oracle)
+        assert out["invalid_pixels"] > 0
+    elif case == "high":
+        sc = scenes.random_tris(40, 32, 150, seed=5, area_median=120.0)
+        _check(sc, VISUALIZE_ERRORS, 48, oracle)
+    else:
+        sc = scenes.random_tris(40, 32, 120, seed=6, area_median=120.0, alpha_range=(0.05, 0.2))
+        _check(sc, 2, 48, oracle)  # additive: segment saturation matters
+
+
+def test_pow_series_accuracy():
+    xs = np.concatenate([np.geomspace(1e-6, 4.0, 400), np.linspace(0.04, 1.0, 200)]).astype(np.float32)
+    for y in (np.float32(2.4), np.float32(1.0) / np.float32(2.4), np.float32(0.5), np.float32(-1.5)):
+        for x in xs:
+            ref = math.pow(float(x), float(y))
+            got = float(pow_series(x, y))
+            # rounding of z = y * log2(x) in float32 grows with |z|; the sRGB domains keep |z| < 20
+            z = abs(float(y) * math.log2(float(x)))
+            assert abs(got - ref) <= (2e-6 + 1e-7 * z) * ref, (x, y, got, ref)
+
+
+def test_ref_order_equals_exact_order_for_flat_layers(oracle):
+    """Triangles parallel to the screen at well separated depths: every block key orders the
+    layers as their depth does, so the window never reorders and the per-pixel order equals the
+    exact mode's."""
+    rng = np.random.default_rng(9)
+    tris, cols = [], []
+    for i in range(40):
+        z = 2.0 + 0.5 * i
+        cx, cy = rng.uniform(0, 64), rng.uniform(0, 48)
+        r = rng.uniform(6, 20)
+        tris.append([(cx - r, cy - r, z), (cx + r, cy - 0.3 * r, z), (cx, cy + r, z)])
+    cols = [[tuple(int(v) for v in rng.integers(0, 256, 4))] * 3 for _ in range(40)]
+    sc = scenes.screen_triangles(tris, cols, 64, 48)
+    a = oracle.run(sc, order_mode=0, max_per_pixel=64)
+    b = oracle.run(sc, order_mode=1, max_per_pixel=64, flags=VISUALIZE_ERRORS)
+    np.testing.assert_array_equal(a["frag_counts"], b["frag_counts"])
+    np.testing.assert_array_equal(a["frag_prims"], b["frag_prims"])
+    assert b["invalid_pixels"] == 0
+
+
+def test_ref_order_rejects_alpha_threshold(oracle):
+    sc = scenes.small_scene(32, 32, 20, seed=1)
+    with pytest.raises(RuntimeError):
+        oracle.run(sc, order_mode=1, flags=4)
