@@ -196,7 +196,14 @@ typedef struct lucid_info {
 #define LUCID_OPT_TIMERS 0x01u            /* clock64 section timers into lucid_info.*_timers */
 #define LUCID_OPT_ADDITIVE_BLENDING 0x02u /* out += rgb*a (shading.glsl:276-277)               */
 #define LUCID_OPT_ALPHA_THRESHOLD 0x04u   /* stop a pixel once T < 1/128 (shading.glsl:62)     */
-#define LUCID_OPT_VISUALIZE_ERRORS 0x08u  /* reserved (reference-order mode only)              */
+#define LUCID_OPT_VISUALIZE_ERRORS 0x08u  /* reference-order mode: depth-4 window, pixels whose
+                                           * samples arrive too far out of order are red and
+                                           * counted in lucid_info.stats[2] (shading.glsl:186-264) */
+#define LUCID_OPT_REFERENCE_ORDER 0x20u   /* the reference's own order and blend instead of the
+                                           * exact order: 22/18-bit block keys, 3-deep depth
+                                           * window, lit sRGB RGBA8 shading (raster_low/high.glsl,
+                                           * shading.glsl); not with ALPHA_THRESHOLD, gradients or
+                                           * batches */
 #define LUCID_OPT_PIXEL_BLEND 0x10u       /* raster pass stores each pixel's sorted fragment
                                            * list; a pixel-parallel kernel shades and blends it
                                            * (same image bits; lucid_autotune picks it per scene) */

@@ -23,7 +23,7 @@ ERR_NAMES = {0: "none", 1: "visible quads", 2: "bin refs", 3: "band entries",
 
 # render option flags
 OPT_TIMERS, OPT_ADDITIVE_BLENDING, OPT_ALPHA_THRESHOLD, OPT_VISUALIZE_ERRORS = 1, 2, 4, 8
-OPT_PIXEL_BLEND = 16
+OPT_PIXEL_BLEND, OPT_REFERENCE_ORDER = 16, 32
 
 # internal buffers of lucid_download_buffer
 BUF_QUAD_AABBS, BUF_TRI_BARY, BUF_TRI_SCAN, BUF_TRI_DEPTH, BUF_QUAD_COLORS = 0, 1, 2, 3, 4

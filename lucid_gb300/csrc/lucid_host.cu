@@ -18,6 +18,7 @@
 
 namespace lucid {
 cudaError_t configureRasterKernel();
+cudaError_t configureRefKernel();
 }
 
 using namespace lucid;
@@ -90,6 +91,7 @@ struct lucid_renderer {
 	int* bin_batches = nullptr;
 	uint32_t* raster_work = nullptr;
 	uint2* band_scratch = nullptr;
+	uint8_t* ref_plan = nullptr; // reference-order mode: path of every bin
 
 	FrameParams last{}; // parameters of the last quad setup (used by the later passes)
 	bool have_frame = false;
@@ -411,8 +413,10 @@ extern "C" lucid_status lucid_create(const lucid_options* options, int32_t width
 	r->opts.binning_ctas = std::min(r->opts.binning_ctas, 4096);
 	r->binning_ctas_alloc = r->opts.binning_ctas;
 	err = configureRasterKernel();
+	if(err == cudaSuccess)
+		err = configureRefKernel();
 	if(err != cudaSuccess)
-		return bail(cudaFail(err, "configure raster kernel"));
+		return bail(cudaFail(err, "configure raster kernels"));
 	int ctas_per_sm = r->opts.raster_ctas_per_sm > 0 ? r->opts.raster_ctas_per_sm : 1;
 	r->raster_ctas = r->num_sms * ctas_per_sm;
 
@@ -437,7 +441,8 @@ extern "C" lucid_status lucid_create(const lucid_options* options, int32_t width
 	   (st = allocate(r, &r->bin_tris, size_t(o.max_bin_refs))) != LUCID_OK ||
 	   (st = allocate(r, &r->bin_batches, size_t(r->opts.binning_ctas) * 2 * r->bin_count)) != LUCID_OK ||
 	   (st = allocate(r, &r->raster_work, size_t(r->bin_count))) != LUCID_OK ||
-	   (st = allocate(r, &r->band_scratch, size_t(r->raster_ctas) * 8 * o.band_capacity)) != LUCID_OK)
+	   (st = allocate(r, &r->band_scratch, size_t(r->raster_ctas) * 8 * o.band_capacity)) != LUCID_OK ||
+	   (st = allocate(r, &r->ref_plan, size_t(r->bin_count))) != LUCID_OK)
 		return bail(st);
 	// zero the records once so that unused slots read as zero in parity dumps
 	for(void* p : {(void*)r->quad_aabbs, (void*)r->quad_source})
@@ -578,6 +583,15 @@ static lucid_status rasterImpl(lucid_renderer* r, const lucid_frame_inputs* in, 
 	p.dump_counts = dump_counts;
 	p.dump_prims = dump_prims;
 	p.dump_max = dump_max;
+	if(r->opts.flags & LUCID_OPT_REFERENCE_ORDER) {
+		if(r->opts.flags & LUCID_OPT_ALPHA_THRESHOLD)
+			return fail(LUCID_NOT_SUPPORTED, "the reference-order mode has no alpha-threshold variant");
+		if((st = resetRasterCounters(r, s)) != LUCID_OK)
+			return st;
+		LUCID_CUDA_TRY(cudaMemsetAsync(&r->info()->stats[2], 0, 4, s));
+		launchRefRaster(p, r->ref_plan, s);
+		return checkLaunch("raster (reference order)");
+	}
 	if((r->opts.flags & LUCID_OPT_PIXEL_BLEND) && !dump_counts)
 		return rasterPixelBlend(r, p, s);
 	if((st = resetRasterCounters(r, s)) != LUCID_OK)
@@ -709,8 +723,8 @@ static lucid_status checkGradInputs(lucid_renderer* r, const lucid_frame_inputs*
 	lucid_status st = validateInputs(r, in);
 	if(st != LUCID_OK)
 		return st;
-	if(r->opts.flags & (LUCID_OPT_ADDITIVE_BLENDING | LUCID_OPT_ALPHA_THRESHOLD))
-		return fail(LUCID_NOT_SUPPORTED, "gradient passes support the front-to-back blend only");
+	if(r->opts.flags & (LUCID_OPT_ADDITIVE_BLENDING | LUCID_OPT_ALPHA_THRESHOLD | LUCID_OPT_REFERENCE_ORDER))
+		return fail(LUCID_NOT_SUPPORTED, "gradient passes support the exact-order front-to-back blend only");
 	if(!r->px_color64) {
 		const size_t npix = size_t(r->width) * r->height;
 		if((st = allocate(r, &r->px_color64, npix * 3)) != LUCID_OK ||
@@ -1122,6 +1136,8 @@ extern "C" lucid_status lucid_render_batch(lucid_renderer* r, const lucid_view* 
 										   int32_t num_views, void* stream) {
 	if(!r || !views || num_views <= 0)
 		return fail(LUCID_INVALID_ARG, "lucid_render_batch: renderer, views and num_views > 0 are required");
+	if(r->opts.flags & (LUCID_OPT_REFERENCE_ORDER | LUCID_OPT_PIXEL_BLEND))
+		return fail(LUCID_NOT_SUPPORTED, "lucid_render_batch renders the exact order with the raster-pass blend");
 	if(num_views > r->opts.max_views || num_views > kMaxBatchViews)
 		return fail(LUCID_CAPACITY_EXCEEDED, "lucid_render_batch: num_views " + std::to_string(num_views) +
 												  " > options.max_views (at most " + std::to_string(kMaxBatchViews) +

@@ -21,6 +21,8 @@ void launchRasterBatch(const FrameParams* views_dev, int num_views, int* level_p
 void launchBlendPixels(const FrameParams& p, cudaStream_t stream);
 void launchGradColor(const FrameParams& p, cudaStream_t stream);
 void launchGradBackward(const FrameParams& p, cudaStream_t stream);
+// Reference-order mode: per-bin path, then one CTA per (bin, 8x4 half-block).
+void launchRefRaster(const FrameParams& p, uint8_t* plan, cudaStream_t stream);
 size_t rasterSmemBytes();
 int rasterThreads();
 

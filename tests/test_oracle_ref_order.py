@@ -25,7 +25,7 @@ def _check(sc, flags, threshold, oracle):
     return out
 
 
-@pytest.mark.parametrize("case", ["low", "low_fp32_opacity_errors", "high", "high_additive"])
+@pytest.mark.parametrize("case", ["low", "low_fp32_opacity_errors", "high", "high_additive", "promoted"])
 def test_ref_order_matches_model(oracle, case):
     if case == "low":
         sc = scenes.small_scene(64, 48, 160, seed=3, area_median=150.0)
@@ -40,9 +40,14 @@ def test_ref_order_matches_model(oracle, case):
     elif case == "high":
         sc = scenes.random_tris(40, 32, 150, seed=5, area_median=120.0)
         _check(sc, VISUALIZE_ERRORS, 48, oracle)
-    else:
+    elif case == "high_additive":
         sc = scenes.random_tris(40, 32, 120, seed=6, area_median=120.0, alpha_range=(0.05, 0.2))
         _check(sc, 2, 48, oracle)  # additive: segment saturation matters
+    else:
+        # LOW by count, but the densest 8x8 block holds > 256 tris: the HIGH path
+        sc = scenes.random_tris(32, 32, 400, seed=34, center_sigma=2.0, area_median=20.0, area_sigma=0.5)
+        out = _check(sc, VISUALIZE_ERRORS, 1024, oracle)
+        assert out["bin_level_counts"][2] == 1
 
 
 def test_pow_series_accuracy():
