@@ -68,6 +68,7 @@ struct FrameParams {
 	int* bin_batches;     // num_binning_ctas * 2 * bin_count histograms
 	uint32_t* raster_work; // bin_count bin ids: HIGH, LOW, EMPTY
 	uint2* band_scratch;  // per raster CTA: 8 * band_capacity entries
+	uint2* band_keys;     // per raster CTA and band entry: depth-key range over the current group
 	int* dump_counts;     // verification mode (may be null)
 	int* dump_prims;
 	int dump_max;

@@ -91,6 +91,7 @@ struct lucid_renderer {
 	int* bin_batches = nullptr;
 	uint32_t* raster_work = nullptr;
 	uint2* band_scratch = nullptr;
+	uint2* band_keys = nullptr;
 	uint8_t* ref_plan = nullptr; // reference-order mode: path of every bin
 
 	FrameParams last{}; // parameters of the last quad setup (used by the later passes)
@@ -209,6 +210,7 @@ FrameParams makeParams(lucid_renderer* r, const lucid_frame_inputs* in, float* o
 	p.bin_batches = r->bin_batches;
 	p.raster_work = r->raster_work;
 	p.band_scratch = r->band_scratch;
+	p.band_keys = r->band_keys;
 	return p;
 }
 
@@ -442,6 +444,7 @@ extern "C" lucid_status lucid_create(const lucid_options* options, int32_t width
 	   (st = allocate(r, &r->bin_batches, size_t(r->opts.binning_ctas) * 2 * r->bin_count)) != LUCID_OK ||
 	   (st = allocate(r, &r->raster_work, size_t(r->bin_count))) != LUCID_OK ||
 	   (st = allocate(r, &r->band_scratch, size_t(r->raster_ctas) * 8 * o.band_capacity)) != LUCID_OK ||
+	   (st = allocate(r, &r->band_keys, size_t(r->raster_ctas) * 8 * o.band_capacity)) != LUCID_OK ||
 	   (st = allocate(r, &r->ref_plan, size_t(r->bin_count))) != LUCID_OK)
 		return bail(st);
 	// zero the records once so that unused slots read as zero in parity dumps
@@ -1029,6 +1032,7 @@ void batchParams(lucid_renderer* r, BatchPlan* b, const lucid_view* views, std::
 		p.bin_batches = b->bin_batches + bbase;
 		p.raster_work = b->raster_work + rbase;
 		p.band_scratch = r->band_scratch;
+		p.band_keys = r->band_keys;
 		p.ref_alloc = b->counters;
 		qbase += size_t(cap);
 		ibase += size_t(in.num_instances) + 1;

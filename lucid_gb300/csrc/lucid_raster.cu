@@ -290,10 +290,16 @@ __device__ void writePixel(const FrameParams& p, int px, int py, float4 c) {
 // rows (lane = pixel column) and split a row's band entries; entries are loaded 32 at a time
 // (one per lane) and broadcast by shuffle. The key is evaluated exactly as in the oracle
 // (shading.glsl:116): dx * px + (dy * py + dz).
+//
+// With `ekeys` (the entries' depth-key ranges over the group, written by the histogram pass)
+// only entries whose range meets the current window of some pixel of the row are visited; the
+// window of pixel t holds the keys of its buckets [px_lo, px_cut] (bucket = (key - kmin) >> shift).
 template <typename Fn>
 __device__ __forceinline__ void forEachGroupFragment(const FrameParams& p, const RasterSmem& s,
 													  const uint2* scratch, int band_cap, int bin_x,
-													  int bin_y, int p0, int p1, Fn fn) {
+													  int bin_y, int p0, int p1, Fn fn,
+													  const uint2* ekeys = nullptr, uint32_t kmin = 0u,
+													  int shift = 0) {
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	const int r0 = p0 >> 5, r1 = (p1 - 1) >> 5;
 	const int nrows = r1 - r0 + 1;
@@ -308,18 +314,40 @@ __device__ __forceinline__ void forEachGroupFragment(const FrameParams& p, const
 	const bool in_group = pix >= p0 && pix < p1;
 	const int t = pix - p0;
 	const float fx = float(bin_x + lane), fy = float(bin_y + row);
+	uint32_t wlo = 0u, whi = 0xffffffffu;
+	if(ekeys) {
+		uint32_t lo_k = 0xffffffffu, hi_k = 0u;
+		if(in_group && s.px_cut[t] >= 0) {
+			const unsigned long long a = (unsigned long long)kmin + ((unsigned long long)s.px_lo[t] << shift);
+			const unsigned long long z = (unsigned long long)kmin + ((unsigned long long)(s.px_cut[t] + 1) << shift) - 1ull;
+			lo_k = uint32_t(a < 0xffffffffull ? a : 0xffffffffull);
+			hi_k = uint32_t(z < 0xffffffffull ? z : 0xffffffffull);
+		}
+#pragma unroll
+		for(int o = 16; o > 0; o >>= 1) {
+			lo_k = min(lo_k, __shfl_xor_sync(0xffffffffu, lo_k, o));
+			hi_k = max(hi_k, __shfl_xor_sync(0xffffffffu, hi_k, o));
+		}
+		if(lo_k > hi_k)
+			return; // no pixel of this row takes part in the window
+		wlo = lo_k, whi = hi_k;
+	}
 	for(int j0 = jbeg; j0 < jend; j0 += 32) {
 		const int j = j0 + lane;
 		uint2 e = make_uint2(0x1fu << 5 * 3, 0u); // empty spans for lanes past the end
 		float dx = 0.0f, dy = 0.0f, dz = 0.0f;
-		if(j < jend) {
+		bool rel = j < jend;
+		if(rel && ekeys) {
+			const uint2 kr = ekeys[size_t(b) * band_cap + j];
+			rel = kr.y >= wlo && kr.x <= whi;
+		}
+		if(rel) {
 			e = scratch[size_t(b) * band_cap + j];
 			uint4 d = __ldg(p.tri_depth + entryTri(e));
 			dx = bitsf(d.x), dy = bitsf(d.y), dz = bitsf(d.z);
 		}
-		const int cnt = min(32, jend - j0);
-#pragma unroll 4
-		for(int k = 0; k < cnt; k++) {
+		for(uint32_t todo = __ballot_sync(0xffffffffu, rel); todo != 0u; todo &= todo - 1u) {
+			const int k = __ffs(todo) - 1;
 			uint32_t ex = __shfl_sync(0xffffffffu, e.x, k), ey = __shfl_sync(0xffffffffu, e.y, k);
 			int lo = (ex >> rshift) & 31, hi = (ey >> rshift) & 31;
 			bool covered = in_group && lane >= lo && lane <= hi;
@@ -415,6 +443,7 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 	const FrameParams& p_first = work.first();
 	const int band_cap = p_first.band_capacity;
 	uint2* scratch = p_first.band_scratch + size_t(blockIdx.x) * 8 * band_cap;
+	uint2* ekeys = p_first.band_keys + size_t(blockIdx.x) * 8 * band_cap;
 	const uint32_t opt_flags = p_first.flags;
 	const bool additive = (opt_flags & LUCID_OPT_ADDITIVE_BLENDING) != 0;
 	const bool alpha_threshold = (opt_flags & LUCID_OPT_ALPHA_THRESHOLD) != 0;
@@ -676,6 +705,7 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 						uint2 e = scratch[size_t(b) * band_cap + j];
 						uint4 d = __ldg(p.tri_depth + entryTri(e));
 						float dx = bitsf(d.x), dy = bitsf(d.y), dz = bitsf(d.z);
+						uint32_t emn = 0xffffffffu, emx = 0u;
 #pragma unroll
 						for(int r = 0; r < 4; r++) {
 							int row = b * 4 + r;
@@ -689,9 +719,17 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 							float ty = dy * float(bin_y + row) + dz;
 							uint32_t ka = nearFirstKey(dx * float(bin_x + xlo) + ty);
 							uint32_t kb = nearFirstKey(dx * float(bin_x + xhi) + ty);
-							kmn = min(kmn, min(ka, kb));
-							kmx = max(kmx, max(ka, kb));
+							emn = min(emn, min(ka, kb));
+							emx = max(emx, max(ka, kb));
 						}
+						kmn = min(kmn, emn);
+						kmx = max(kmx, emx);
+						// the entry's key range over the group, for the windows' entry culling;
+						// planes that could evaluate to NaN somewhere keep the full range
+						const float lim = 1e30f;
+						if(!(fabsf(dx) < lim && fabsf(dy) < lim && fabsf(dz) < lim))
+							emn = 0u, emx = 0xffffffffu;
+						ekeys[size_t(b) * band_cap + j] = make_uint2(emn, emx);
 					}
 				}
 #pragma unroll
@@ -840,7 +878,8 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 												 s.kv[0][0][pos] = key;
 												 s.kv[0][1][pos] = uint32_t(tp) | (uint32_t(b) << 8) | (uint32_t(j) << 11);
 											 }
-										 });
+										 },
+										 windowed ? ekeys : nullptr, kmin, shift);
 				}
 				__syncthreads();
 				// every window segment must be exactly full (histogram and generation evaluate the
