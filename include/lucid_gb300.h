@@ -414,6 +414,21 @@ typedef struct lucid_tuning {
 lucid_status lucid_autotune(lucid_renderer* renderer, const lucid_frame_inputs* inputs,
 							float* scratch_rgba, lucid_tuning* out, void* stream);
 
+/* Quad generator (replaces triNeighbours / quadNodes / genQuads, src/quad_generator.cpp:18-201,
+ * as used by Scene::generateQuads, src/scene.cpp:237-246): pairs triangles that share an edge
+ * into quads, the quads_ib format of lucid_frame_inputs. positions: device, num_verts x float3;
+ * tris: device, num_tris x 3 vertex indices; out_quads: device, capacity num_tris x 4 u32.
+ * Writes, in tri order, each tri's selected quad {a, opposite, b, c}, nothing for the second
+ * tri of a selected quad, or the degenerate quad (a, b, c, c); *out_num_quads (host) receives the
+ * count, *out_num_degenerate (host, may be NULL) the degenerate ones. Quads are chosen by a greedy
+ * independent set over score = conflicts - squareness * square_weight (the reference's weight is
+ * 1.0, src/scene_convert.cpp:36) taken in the fixed order of the initial scores (ties by quad
+ * index); the reference lowers scores as the greedy proceeds, which is sequential. Synchronous;
+ * allocates its scratch. LUCID_INVALID_ARG for a vertex index outside [0, num_verts). */
+lucid_status lucid_quad_generate(const float* positions, int32_t num_verts, const int32_t* tris,
+								 int32_t num_tris, float square_weight, uint32_t* out_quads,
+								 int32_t* out_num_quads, int32_t* out_num_degenerate, void* stream);
+
 /* ---------------------------------------------------------------------------------------- */
 /* Binning without allocation. No counterpart in the reference.
  *

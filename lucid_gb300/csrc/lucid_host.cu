@@ -1185,6 +1185,29 @@ extern "C" lucid_status lucid_render_batch(lucid_renderer* r, const lucid_view* 
 	return LUCID_OK;
 }
 
+extern "C" lucid_status lucid_quad_generate(const float* positions, int32_t num_verts, const int32_t* tris,
+											int32_t num_tris, float square_weight, uint32_t* out_quads,
+											int32_t* out_num_quads, int32_t* out_num_degenerate, void* stream) {
+	if(!out_num_quads || num_tris < 0 || num_verts < 0 || (num_tris > 0 && (!positions || !tris || !out_quads)))
+		return fail(LUCID_INVALID_ARG, "lucid_quad_generate: bad arguments");
+	if(int64_t(num_tris) * 6 > int64_t(1) << 31)
+		return fail(LUCID_CAPACITY_EXCEEDED, "lucid_quad_generate: too many triangles");
+	std::string err;
+	int nq = 0, nd = 0;
+	const int rc = quadGenerate(positions, num_verts, tris, num_tris, square_weight, out_quads, &nq, &nd,
+								reinterpret_cast<cudaStream_t>(stream), err);
+	if(rc == 1)
+		return fail(LUCID_INVALID_ARG, err);
+	if(rc == 2)
+		return fail(LUCID_OUT_OF_MEMORY, err);
+	if(rc != 0)
+		return fail(LUCID_CUDA_ERROR, err);
+	*out_num_quads = nq;
+	if(out_num_degenerate)
+		*out_num_degenerate = nd;
+	return LUCID_OK;
+}
+
 extern "C" lucid_status lucid_get_batch_info(lucid_renderer* r, int32_t view, lucid_info* out, void* stream) {
 	if(!r || !out || !r->batch || view < 0 || view >= r->batch->num_views)
 		return fail(LUCID_INVALID_ARG, "lucid_get_batch_info: no such view of the last batch");

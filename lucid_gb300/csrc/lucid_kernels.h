@@ -1,6 +1,8 @@
 // Launchers of the lucid_gb300 kernels (one per reference compute pass).
 #pragma once
 
+#include <string>
+
 #include "lucid_common.cuh"
 
 namespace lucid {
@@ -23,6 +25,10 @@ void launchGradColor(const FrameParams& p, cudaStream_t stream);
 void launchGradBackward(const FrameParams& p, cudaStream_t stream);
 // Reference-order mode: per-bin path, then one CTA per (bin, 8x4 half-block).
 void launchRefRaster(const FrameParams& p, uint8_t* plan, cudaStream_t stream);
+// Quad generator (synchronous on `stream`): 0 ok, 1 bad vertex index, 2 out of memory, 3 CUDA error.
+int quadGenerate(const float* positions, int num_verts, const int32_t* tris, int num_tris, float square_weight,
+				 uint32_t* out_quads, int* out_num_quads, int* out_num_degenerate, cudaStream_t stream,
+				 std::string& err);
 size_t rasterSmemBytes();
 int rasterThreads();
 

@@ -260,3 +260,18 @@ class LucidRenderer:
             max_pixel_fragments=int(info.max_pixel_fragments),
             error=_lib.ERR_NAMES.get(info.error_code, str(info.error_code)),
             error_detail=tuple(info.error_detail))
+
+
+def quad_generate(positions, tris, square_weight: float = 1.0, stream=None):
+    """Pairs triangles into quads on the GPU (lucid_quad_generate). positions: (V, 3) float32 and
+    tris: (T, 3) int32 CUDA tensors. Returns (quads (n, 4) uint32-as-int32 CUDA tensor,
+    num_degenerate)."""
+    lib = _lib.load()
+    positions = positions.contiguous()
+    tris = tris.contiguous()
+    out = torch.empty((max(1, tris.shape[0]), 4), dtype=torch.int32, device=tris.device)
+    n, nd = ctypes.c_int32(), ctypes.c_int32()
+    check(lib.lucid_quad_generate(_dptr(positions), int(positions.shape[0]), _dptr(tris), int(tris.shape[0]),
+                                  float(square_weight), _dptr(out), ctypes.byref(n), ctypes.byref(nd),
+                                  _stream_ptr(stream)), "lucid_quad_generate")
+    return out[:n.value], nd.value

@@ -308,6 +308,28 @@ def _grid_quads(nu, nv, base):
     return np.array(quads, dtype=np.uint32)
 
 
+def tri_mesh(kind="sphere", nu=64, nv=32, seed=0, noise=0.01, shuffle=True):
+    """Triangle mesh for the quad generator: a sphere or plane grid whose cells are split into two
+    triangles along a random diagonal, vertices jittered by `noise`, triangles in random order
+    (shuffle) or grid order. Returns (positions float32 [V, 3], tris int32 [T, 3])."""
+    rng = np.random.default_rng(seed)
+    pts = _sphere_grid(nu, nv) if kind == "sphere" else _plane_grid(nu, nv)
+    pos = pts.reshape(-1, 3) + rng.normal(0.0, noise, size=(pts.shape[0] * pts.shape[1], 3))
+    tris = []
+    for j in range(nv):
+        for i in range(nu):
+            a = j * (nu + 1) + i
+            b, c, d = a + 1, a + 1 + (nu + 1), a + (nu + 1)
+            if rng.random() < 0.5:
+                tris += [(a, b, c), (a, c, d)]
+            else:
+                tris += [(a, b, d), (b, c, d)]
+    tris = np.array(tris, np.int32)
+    if shuffle:
+        tris = tris[rng.permutation(len(tris))]
+    return pos.astype(np.float32), tris
+
+
 def _rotation(rng):
     q = rng.normal(size=4)
     q /= np.linalg.norm(q)

@@ -227,3 +227,24 @@ class GradModel:
         op = None if opacity is None else np.ascontiguousarray(opacity, np.float64)
         tg = np.ascontiguousarray(target, np.float32)
         return float(self.L.oracle_grad_fd(self.ctx, vc.ctypes.data, _ptr(op), tg.ctypes.data, kind, index, h))
+
+
+def quadgen(positions, tris, square_weight=1.0, order=0):
+    """Quad generator (oracle_quadgen): order 0 = the reference's greedy, 1 = fixed order.
+    Returns (quads uint32 [n, 4], num_degenerate)."""
+    L = lib()
+    if not hasattr(L, "_qg_bound"):
+        L.oracle_quadgen.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_float,
+                                     ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32),
+                                     ctypes.POINTER(ctypes.c_int32)]
+        L.oracle_quadgen.restype = ctypes.c_int
+        L._qg_bound = True
+    pos = np.ascontiguousarray(positions, np.float32)
+    tr = np.ascontiguousarray(tris, np.int32)
+    out = np.zeros((max(1, tr.shape[0]), 4), np.uint32)
+    n, nd = ctypes.c_int32(), ctypes.c_int32()
+    rc = L.oracle_quadgen(pos.ctypes.data, pos.shape[0], tr.ctypes.data, tr.shape[0], float(square_weight), order,
+                          out.ctypes.data, ctypes.byref(n), ctypes.byref(nd))
+    if rc != 0:
+        raise RuntimeError(f"oracle_quadgen failed ({rc})")
+    return out[:n.value], nd.value

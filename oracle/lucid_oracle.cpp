@@ -16,6 +16,8 @@
 #include <cstring>
 #include <thread>
 #include <vector>
+#include <unordered_map>
+#include <set>
 
 namespace {
 
@@ -1598,6 +1600,255 @@ extern "C" double oracle_grad_fd(void* ctx, const double* vc, const double* op, 
 	for(uint32_t pix : pixels)
 		lm += pixelLoss64(g, pix, v.data(), g.has_opacity ? o.data() : nullptr, target);
 	return (lp - lm) / (2.0 * h);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Quad generator (src/quad_generator.cpp): pairs triangles that share an edge into quads.
+//
+// triNeighbours (:18-44): neighbour across edge j of tri i is the first tri (lowest index) that
+// holds the reversed directed edge, unless that is tri i itself. quadNodes (:55-120): for every
+// tri in order and edge i whose neighbour also lists it, with a vertex not in the tri, one quad
+// {tri[i], opposite, tri[i+1], tri[i+2]} (created by the lower-index tri of the pair), its
+// squareness (:8-16) and conflicts with the other quads of both tris. genQuads (:122-201): a
+// greedy independent set by score = conflicts - squareness * square_weight, then every tri in
+// order gives its selected quad, or a degenerate quad (a, b, c, c); the second tri of a selected
+// quad gives nothing.
+// Two greedy variants: order 0 is the reference's (a heap that lowers the score of quads whose
+// conflicts are removed, :154-171; equal scores by quad index, fwk's heap order being unknown);
+// order 1 takes the same scores in synchronous rounds: the candidates are the undecided quads
+// with the lowest number of undecided conflicts (the heap's leading term), and every candidate
+// whose (score on the undecided conflicts, index) is below that of each conflicting candidate is
+// selected at once. The CUDA path computes it in parallel; on the test meshes it leaves as few
+// tris unpaired as the reference's order. normalize(v) = v / |v|; a NaN squareness counts as 0.
+
+namespace {
+
+struct QNode {
+	int tris[2];
+	int verts[4];
+	int conflicts[4];
+	float squareness;
+	int degree() const {
+		int d = 0;
+		for(int c : conflicts)
+			d += c != -1;
+		return d;
+	}
+	void addConflict(int idx) {
+		for(int c : conflicts)
+			if(c == idx)
+				return;
+		for(int& c : conflicts)
+			if(c == -1) {
+				c = idx;
+				return;
+			}
+	}
+};
+
+V3 normalize3(V3 v) {
+	const float l = sqrtf(dot(v, v));
+	return v3(v.x / l, v.y / l, v.z / l);
+}
+
+float quadSquareness(const V3 c[4]) {
+	V3 e[4];
+	for(int i = 0; i < 4; i++)
+		e[i] = normalize3(sub(c[(i + 1) & 3], c[i]));
+	float out = 0.0f;
+	for(int i = 0; i < 4; i++)
+		out += fabsf(dot(e[i], e[(i + 1) & 3]));
+	const float sq = (4.0f - out) * 0.25f;
+	return sq == sq ? sq : 0.0f;
+}
+
+} // namespace
+
+extern "C" int oracle_quadgen(const float* positions, int num_verts, const int32_t* tris, int num_tris,
+							  float square_weight, int order, uint32_t* out_quads, int32_t* out_num_quads,
+							  int32_t* out_num_degenerate) {
+	if(num_tris < 0 || (num_tris > 0 && (!tris || !positions || !out_quads)) || order < 0 || order > 1)
+		return 1;
+	for(int i = 0; i < 3 * num_tris; i++)
+		if(tris[i] < 0 || tris[i] >= num_verts)
+			return 2;
+	const size_t nt = size_t(num_tris);
+	// triNeighbours
+	std::unordered_map<uint64_t, int> edge_tri;
+	edge_tri.reserve(nt * 4);
+	auto ekey = [](int a, int b) { return (uint64_t(uint32_t(a)) << 32) | uint32_t(b); };
+	for(size_t i = 0; i < nt; i++)
+		for(int j = 0; j < 3; j++)
+			edge_tri.emplace(ekey(tris[i * 3 + j], tris[i * 3 + (j == 2 ? 0 : j + 1)]), int(i));
+	std::vector<int> nb(nt * 3, -1);
+	for(size_t i = 0; i < nt; i++)
+		for(int j = 0; j < 3; j++) {
+			auto it = edge_tri.find(ekey(tris[i * 3 + (j == 2 ? 0 : j + 1)], tris[i * 3 + j]));
+			if(it != edge_tri.end() && it->second != int(i))
+				nb[i * 3 + j] = it->second;
+		}
+	// quadNodes
+	std::vector<QNode> quads;
+	std::vector<int> tri_quads(nt * 3, -1);
+	auto vpos = [&](int v) { return xyz(positions + size_t(v) * 3); };
+	for(size_t i0 = 0; i0 < nt; i0++) {
+		const int* t0 = tris + i0 * 3;
+		for(int i = 0; i < 3; i++) {
+			const int i1 = nb[i0 * 3 + i];
+			if(i1 == -1 || tri_quads[i0 * 3 + i] != -1)
+				continue;
+			int j = -1;
+			for(int k = 0; k < 3; k++)
+				if(nb[size_t(i1) * 3 + k] == int(i0)) {
+					j = k;
+					break;
+				}
+			if(j == -1)
+				continue;
+			int opposite = -1;
+			for(int k = 0; k < 3; k++) {
+				const int ov = tris[size_t(i1) * 3 + k];
+				if(ov != t0[0] && ov != t0[1] && ov != t0[2]) {
+					opposite = ov;
+					break;
+				}
+			}
+			if(opposite == -1)
+				continue;
+			QNode q;
+			q.tris[0] = int(i0), q.tris[1] = i1;
+			q.verts[0] = t0[i], q.verts[1] = opposite, q.verts[2] = t0[(i + 1) % 3], q.verts[3] = t0[(i + 2) % 3];
+			for(int& c : q.conflicts)
+				c = -1;
+			V3 pts[4];
+			for(int k = 0; k < 4; k++)
+				pts[k] = vpos(q.verts[k]);
+			q.squareness = quadSquareness(pts);
+			const int qi = int(quads.size());
+			quads.push_back(q);
+			tri_quads[i0 * 3 + i] = qi;
+			tri_quads[size_t(i1) * 3 + j] = qi;
+		}
+	}
+	for(size_t t = 0; t < nt; t++)
+		for(int i = 0; i < 3; i++) {
+			const int q0 = tri_quads[t * 3 + i], q1 = tri_quads[t * 3 + (i == 2 ? 0 : i + 1)];
+			if(q0 != -1 && q1 != -1) {
+				quads[size_t(q0)].addConflict(q1);
+				quads[size_t(q1)].addConflict(q0);
+			}
+		}
+	// genQuads: greedy independent set
+	const size_t nq = quads.size();
+	std::vector<uint8_t> state(nq, 0); // 2 selected, 1 removed
+	std::vector<bool> second_tri(nt, false);
+	std::vector<int> degree(nq);
+	for(size_t q = 0; q < nq; q++)
+		degree[q] = quads[q].degree();
+	auto score = [&](size_t q) { return float(degree[q]) - quads[q].squareness * square_weight; };
+	auto select = [&](size_t q) {
+		state[q] = 2;
+		second_tri[size_t(quads[q].tris[1])] = true;
+	};
+	if(order == 1) {
+		// synchronous rounds: every undecided quad scores its undecided conflicts; the candidates
+		// are the undecided quads of the lowest live conflict count, and every candidate whose
+		// (score, index) is below that of each conflicting candidate is selected at once, its
+		// conflicts removed
+		std::vector<std::pair<float, int>> key(nq);
+		std::vector<int> live_deg(nq, 0);
+		std::vector<size_t> picked;
+		size_t undecided = nq;
+		while(undecided > 0) {
+			int min_deg = 5;
+			for(size_t q = 0; q < nq; q++) {
+				if(state[q])
+					continue;
+				int live = 0;
+				for(int c : quads[q].conflicts)
+					live += c != -1 && !state[size_t(c)];
+				live_deg[q] = live;
+				min_deg = std::min(min_deg, live);
+				float sc = float(live) - quads[q].squareness * square_weight;
+				key[q] = {sc == 0.0f ? 0.0f : sc, int(q)};
+			}
+			auto candidate = [&](size_t q) { return !state[q] && live_deg[q] == min_deg; };
+			picked.clear();
+			for(size_t q = 0; q < nq; q++) {
+				if(!candidate(q))
+					continue;
+				bool local_min = true;
+				for(int c : quads[q].conflicts)
+					if(c != -1 && candidate(size_t(c)) && !(key[q] < key[size_t(c)]))
+						local_min = false;
+				if(local_min)
+					picked.push_back(q);
+			}
+			for(size_t q : picked) {
+				select(q);
+				for(int c : quads[q].conflicts)
+					if(c != -1)
+						state[size_t(c)] = 1;
+			}
+			undecided = 0;
+			for(size_t q = 0; q < nq; q++)
+				undecided += state[q] == 0;
+		}
+	} else {
+		std::set<std::pair<float, int>> heap;
+		std::vector<float> key(nq);
+		for(size_t q = 0; q < nq; q++) {
+			key[q] = score(q);
+			heap.insert({key[q], int(q)});
+		}
+		while(!heap.empty()) {
+			const size_t q = size_t(heap.begin()->second);
+			heap.erase(heap.begin());
+			if(state[q])
+				continue;
+			select(q);
+			for(int c : quads[q].conflicts) {
+				if(c == -1)
+					continue;
+				state[size_t(c)] = 1;
+				for(int c2 : quads[size_t(c)].conflicts)
+					if(c2 != -1 && !state[size_t(c2)]) {
+						degree[size_t(c2)]--;
+						heap.erase({key[size_t(c2)], c2});
+						key[size_t(c2)] = score(size_t(c2));
+						heap.insert({key[size_t(c2)], c2});
+					}
+			}
+		}
+	}
+	// output in tri order
+	int nout = 0, ndeg = 0;
+	for(size_t t = 0; t < nt; t++) {
+		if(second_tri[t])
+			continue;
+		int sel = -1;
+		for(int i = 0; i < 3; i++) {
+			const int q = tri_quads[t * 3 + i];
+			if(q != -1 && state[size_t(q)] == 2) {
+				sel = q;
+				break;
+			}
+		}
+		uint32_t* o = out_quads + size_t(nout) * 4;
+		if(sel == -1) {
+			o[0] = uint32_t(tris[t * 3]), o[1] = uint32_t(tris[t * 3 + 1]);
+			o[2] = uint32_t(tris[t * 3 + 2]), o[3] = uint32_t(tris[t * 3 + 2]);
+			ndeg++;
+		} else {
+			for(int k = 0; k < 4; k++)
+				o[k] = uint32_t(quads[size_t(sel)].verts[k]);
+		}
+		nout++;
+	}
+	*out_num_quads = nout;
+	if(out_num_degenerate)
+		*out_num_degenerate = ndeg;
+	return 0;
 }
 
 extern "C" int oracle_run(const oracle_inputs* in, oracle_outputs* out) {

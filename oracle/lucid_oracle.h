@@ -114,6 +114,17 @@ double oracle_grad_fd(void* ctx, const double* vcolors, const double* opacity, c
 					  int kind, int index, double h);
 uint64_t oracle_grad_num_fragments(void* ctx);
 
+/* ---- quad generator (src/quad_generator.cpp) ----
+ * Pairs triangles (num_tris x 3 vertex indices) that share an edge into quads; out_quads
+ * (capacity num_tris x 4) receives, in tri order, each selected quad or a degenerate quad
+ * (a, b, c, c). order 0: the reference's greedy (heap re-scoring removed quads' neighbours);
+ * order 1: the same scores in synchronous rounds of local minima among the quads of the lowest
+ * live conflict count (the CUDA path's). Returns 0, or
+ * 1 for bad arguments, 2 for a vertex index out of range. */
+int oracle_quadgen(const float* positions, int num_verts, const int32_t* tris, int num_tris,
+				   float square_weight, int order, uint32_t* out_quads, int32_t* out_num_quads,
+				   int32_t* out_num_degenerate);
+
 #ifdef __cplusplus
 }
 #endif
