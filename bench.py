@@ -323,6 +323,35 @@ def batch_bench(steps, warmup, flush_buf, num_views=64):
             "view_errors": errors, "median_of": steps}
 
 
+def quadgen_bench(steps, warmup):
+    """Quad generation (lucid_quad_generate) on a 500k-triangle jittered grid mesh in random
+    triangle order, against the oracle's restatement of the reference's sequential greedy
+    (src/quad_generator.cpp) on one host core."""
+    import time
+    import torch
+    from lucid_gb300 import scenes
+    from lucid_gb300.renderer import quad_generate
+    from oracle import binding as oracle
+    pos, tris = scenes.tri_mesh("plane", 500, 500, seed=21)
+    pos_d, tris_d = torch.from_numpy(pos).cuda(), torch.from_numpy(tris).cuda()
+    for _ in range(warmup):
+        quad_generate(pos_d, tris_d)
+    ms = []
+    for _ in range(steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        q, nd = quad_generate(pos_d, tris_d)
+        torch.cuda.synchronize()
+        ms.append((time.perf_counter() - t0) * 1e3)
+    t0 = time.perf_counter()
+    ref, ref_nd = oracle.quadgen(pos, tris, 1.0, 0)
+    cpu_ms = (time.perf_counter() - t0) * 1e3
+    return {"workload": "500x500 grid, 500k triangles in random order, square_weight 1.0",
+            "triangles": int(tris.shape[0]), "gpu_ms": float(np.median(ms)), "quads": int(q.shape[0]),
+            "degenerate": int(nd), "cpu_reference_greedy_ms": cpu_ms, "cpu_quads": int(ref.shape[0]),
+            "cpu_degenerate": int(ref_nd), "cpu_cores": 1, "median_of": steps}
+
+
 def main():
     args = parse_args()
     rank, world, local = dist_setup(args.gpus)
@@ -442,6 +471,7 @@ def main():
     extras = rank == 0 and not args.no_extras
     fwd_bwd = grad_bench(max(5, args.steps), max(3, args.warmup), flush_buf) if extras else None
     batch = batch_bench(max(5, args.steps), max(3, args.warmup), flush_buf) if extras else None
+    quadgen = quadgen_bench(max(3, min(args.steps, 5)), 1) if extras else None
 
     # ---- CPU baseline (rank 0, N=1 only)
     cpu = None
@@ -479,6 +509,7 @@ def main():
             "mtri_per_s": scene.num_tris * args.steps * world / (total_ms / 1e3) / 1e6,  # equal tris per rank
             "fwd_bwd": fwd_bwd,
             "batch": batch,
+            "quadgen": quadgen,
         }
         print(json.dumps(line), flush=True)
     r.close()
