@@ -422,13 +422,16 @@ int quadGenerate(const float* positions, int num_verts, const int32_t* tris, int
 	if(nq > 0) {
 		qgConflicts<<<gq, kQgThreads, 0, s>>>(quads, nq, tri_quads);
 		// rounds until every quad is decided (each round picks at least the first undecided quad
-		// of the order, so nq rounds bound it)
-		for(int round = 0; round <= nq; round++) {
-			cudaMemsetAsync(counters, 0x7f, 4, s); // [0] lowest live conflict count
+		// of the order, so nq rounds bound it); the host checks after every 16 rounds (rounds
+		// after the last decision change nothing)
+		for(int round = 0; round <= nq; round += 16) {
+			for(int k = 0; k < 16; k++) {
+				cudaMemsetAsync(counters, 0x7f, 4, s); // [0] lowest live conflict count
+				qgScore<<<gq, kQgThreads, 0, s>>>(quads, nq, state, square_weight, live_deg, counters);
+				qgPick<<<gq, kQgThreads, 0, s>>>(quads, nq, state, live_deg, counters, picked);
+				qgApply<<<gq, kQgThreads, 0, s>>>(quads, nq, state, picked, counters + 1);
+			}
 			cudaMemsetAsync(counters + 1, 0, 4, s); // [1] undecided
-			qgScore<<<gq, kQgThreads, 0, s>>>(quads, nq, state, square_weight, live_deg, counters);
-			qgPick<<<gq, kQgThreads, 0, s>>>(quads, nq, state, live_deg, counters, picked);
-			qgApply<<<gq, kQgThreads, 0, s>>>(quads, nq, state, picked, counters + 1);
 			qgCountUndecided<<<gq, kQgThreads, 0, s>>>(state, nq, counters + 1);
 			int undecided = 0;
 			cudaMemcpyAsync(&undecided, counters + 1, 4, cudaMemcpyDeviceToHost, s);
