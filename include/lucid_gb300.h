@@ -246,7 +246,24 @@ typedef struct lucid_frame_inputs {
 	const uint32_t* instance_colors; /* RGBA8 per instance (used with LUCID_INST_HAS_COLOR)     */
 	const float* tri_opacity;        /* optional: per input triangle (quad*2+second), may be 0  */
 	const lucid_config* config;      /* HOST pointer, copied into the renderer's buffer         */
+	/* optional shading inputs (shading.glsl:125-176; NULL when no instance uses them):        */
+	const float* tex_coords;         /* float2 per vertex (LUCID_INST_HAS_ALBEDO_TEXTURE)       */
+	const float* instance_uv_rects;  /* float4 per instance: uv min, uv size (LUCID_INST_HAS_UV_RECT) */
+	const uint32_t* normals;         /* encoded normal per vertex (LUCID_INST_HAS_VERTEX_NORMALS:
+	                                  * 10 bits per axis, (v - 512) / 511, funcs.glsl:61-66)    */
+	const struct lucid_texture* opaque_texture;      /* HOST pointers to texture descriptors */
+	const struct lucid_texture* transparent_texture;
 } lucid_frame_inputs;
+
+/* RGBA8 texture with its mip chain (the reference's opaque / transparent albedo atlases). texels:
+ * device, the levels back to back, level l is max(1, width >> l) x max(1, height >> l) u32
+ * (red in the low byte). Sampled trilinearly with repeat addressing. */
+typedef struct lucid_texture {
+	const uint32_t* texels;
+	int32_t width, height;
+	int32_t num_levels;
+	int32_t _pad;
+} lucid_texture;
 
 /* Draw call of the host-side instance builder (SceneDrawCall, src/lucid_base.h:44-50). */
 typedef struct lucid_draw_call {

@@ -39,11 +39,18 @@ class Options(ctypes.Structure):
                 ("grad_store_fragments", c_int32), ("reserved", c_int32 * 4)]
 
 
+class TextureC(ctypes.Structure):
+    _fields_ = [("texels", c_void_p), ("width", c_int32), ("height", c_int32), ("num_levels", c_int32),
+                ("_pad", c_int32)]
+
+
 class FrameInputsC(ctypes.Structure):
     _fields_ = [("positions", c_void_p), ("colors", c_void_p), ("color_format", c_int32),
                 ("num_verts", c_int32), ("quads_ib", c_void_p), ("num_quads", c_int32),
                 ("num_instances", c_int32), ("instances", c_void_p),
-                ("instance_colors", c_void_p), ("tri_opacity", c_void_p), ("config", c_void_p)]
+                ("instance_colors", c_void_p), ("tri_opacity", c_void_p), ("config", c_void_p),
+                ("tex_coords", c_void_p), ("instance_uv_rects", c_void_p), ("normals", c_void_p),
+                ("opaque_texture", c_void_p), ("transparent_texture", c_void_p)]
 
 
 class Info(ctypes.Structure):

@@ -34,6 +34,10 @@ struct FrameParams {
 	const lucid_instance* instances;
 	const uint32_t* instance_colors;
 	const float* tri_opacity;
+	const float2* tex_coords;       // optional shading inputs
+	const float4* instance_uv_rects;
+	const uint32_t* normals;
+	lucid_texture opaque_tex, trans_tex; // texels null when absent
 	float* out_rgba;
 	// ---- dimensions & limits ----
 	int width, height;
@@ -59,6 +63,8 @@ struct FrameParams {
 	uint32_t* quad_source;
 	uint4* quad_verts;
 	uint4* quad_colors;
+	uint4* quad_normals;  // encoded vertex normals per quad slot (STORAGE_QUAD_NORMAL)
+	uint4* quad_tex;      // 2 per quad slot: tex0, tex1 - tex0, tex2 - tex0, tex3 - tex0
 	uint4* tri_bary;  // 2 per tri
 	uint4* tri_scan;  // 2 per tri
 	uint4* tri_depth; // 1 per tri

@@ -82,6 +82,8 @@ struct lucid_renderer {
 	uint32_t* quad_source = nullptr;
 	uint4* quad_verts = nullptr;
 	uint4* quad_colors = nullptr;
+	uint4* quad_normals = nullptr;
+	uint4* quad_tex = nullptr;
 	uint4* tri_bary = nullptr;
 	uint4* tri_scan = nullptr;
 	uint4* tri_depth = nullptr;
@@ -165,7 +167,18 @@ lucid_status validateInputs(const lucid_renderer* r, const lucid_frame_inputs* i
 		return fail(LUCID_INVALID_ARG, "unknown color_format");
 	if(in->num_quads > 0 && !in->colors)
 		return fail(LUCID_INVALID_ARG, "colors is NULL");
+	for(const lucid_texture* t : {in->opaque_texture, in->transparent_texture})
+		if(t && t->texels && (t->width <= 0 || t->height <= 0 || t->num_levels <= 0 || t->num_levels > 16))
+			return fail(LUCID_INVALID_ARG, "texture size or level count out of range");
 	return LUCID_OK;
+}
+
+void setShadingInputs(FrameParams& p, const lucid_frame_inputs* in) {
+	p.tex_coords = reinterpret_cast<const float2*>(in->tex_coords);
+	p.instance_uv_rects = reinterpret_cast<const float4*>(in->instance_uv_rects);
+	p.normals = in->normals;
+	p.opaque_tex = in->opaque_texture ? *in->opaque_texture : lucid_texture{};
+	p.trans_tex = in->transparent_texture ? *in->transparent_texture : lucid_texture{};
 }
 
 FrameParams makeParams(lucid_renderer* r, const lucid_frame_inputs* in, float* out) {
@@ -180,6 +193,7 @@ FrameParams makeParams(lucid_renderer* r, const lucid_frame_inputs* in, float* o
 	p.instances = in->instances;
 	p.instance_colors = in->instance_colors;
 	p.tri_opacity = in->tri_opacity;
+	setShadingInputs(p, in);
 	p.out_rgba = out;
 	p.cfg = *in->config;
 	p.width = r->width, p.height = r->height;
@@ -201,6 +215,8 @@ FrameParams makeParams(lucid_renderer* r, const lucid_frame_inputs* in, float* o
 	p.quad_source = r->quad_source;
 	p.quad_verts = r->quad_verts;
 	p.quad_colors = r->quad_colors;
+	p.quad_normals = r->quad_normals;
+	p.quad_tex = r->quad_tex;
 	p.tri_bary = r->tri_bary;
 	p.tri_scan = r->tri_scan;
 	p.tri_depth = r->tri_depth;
@@ -435,6 +451,8 @@ extern "C" lucid_status lucid_create(const lucid_options* options, int32_t width
 	   (st = allocate(r, &r->quad_source, mvq)) != LUCID_OK ||
 	   (st = allocate(r, &r->quad_verts, mvq)) != LUCID_OK ||
 	   (st = allocate(r, &r->quad_colors, mvq)) != LUCID_OK ||
+	   (st = allocate(r, &r->quad_normals, mvq)) != LUCID_OK ||
+	   (st = allocate(r, &r->quad_tex, 2 * mvq)) != LUCID_OK ||
 	   (st = allocate(r, &r->tri_bary, 4 * mvq)) != LUCID_OK ||
 	   (st = allocate(r, &r->tri_scan, 4 * mvq)) != LUCID_OK ||
 	   (st = allocate(r, &r->tri_depth, 2 * mvq)) != LUCID_OK ||
@@ -578,6 +596,7 @@ static lucid_status rasterImpl(lucid_renderer* r, const lucid_frame_inputs* in, 
 	p.color_format = in->color_format;
 	p.instance_colors = in->instance_colors;
 	p.tri_opacity = in->tri_opacity;
+	setShadingInputs(p, in);
 	p.cfg.background_color[0] = in->config->background_color[0];
 	p.cfg.background_color[1] = in->config->background_color[1];
 	p.cfg.background_color[2] = in->config->background_color[2];
@@ -998,6 +1017,7 @@ void batchParams(lucid_renderer* r, BatchPlan* b, const lucid_view* views, std::
 		p.instances = in.instances;
 		p.instance_colors = in.instance_colors;
 		p.tri_opacity = in.tri_opacity;
+		setShadingInputs(p, &in);
 		p.out_rgba = vw.out_rgba;
 		p.cfg = *in.config;
 		p.width = vw.width, p.height = vw.height;
@@ -1023,6 +1043,8 @@ void batchParams(lucid_renderer* r, BatchPlan* b, const lucid_view* views, std::
 		p.quad_source = r->quad_source + qbase;
 		p.quad_verts = r->quad_verts + qbase;
 		p.quad_colors = r->quad_colors + qbase;
+		p.quad_normals = r->quad_normals + qbase;
+		p.quad_tex = r->quad_tex + 2 * qbase;
 		p.tri_bary = r->tri_bary + 4 * qbase;
 		p.tri_scan = r->tri_scan + 4 * qbase;
 		p.tri_depth = r->tri_depth + 2 * qbase;

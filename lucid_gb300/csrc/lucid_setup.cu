@@ -424,6 +424,18 @@ template <class Src> __global__ void __launch_bounds__(kSetupThreads) setupStore
 		p.quad_colors[slot] =
 			make_uint4(__ldg(cols + v[0]), __ldg(cols + v[1]), __ldg(cols + v[2]), __ldg(cols + v[3]));
 	}
+	// storeQuad (quad_setup.glsl:256-272): vertex normals, texture coordinates relative to the
+	// first vertex
+	if((flags & LUCID_INST_HAS_VERTEX_NORMALS) && p.normals)
+		p.quad_normals[slot] =
+			make_uint4(__ldg(p.normals + v[0]), __ldg(p.normals + v[1]), __ldg(p.normals + v[2]), __ldg(p.normals + v[3]));
+	if((flags & LUCID_INST_HAS_ALBEDO_TEXTURE) && p.tex_coords) {
+		const float2 t0 = __ldg(p.tex_coords + v[0]), a = __ldg(p.tex_coords + v[1]);
+		const float2 b = __ldg(p.tex_coords + v[2]), c = __ldg(p.tex_coords + v[3]);
+		p.quad_tex[size_t(slot) * 2] = make_uint4(fbits(t0.x), fbits(t0.y), fbits(a.x - t0.x), fbits(a.y - t0.y));
+		p.quad_tex[size_t(slot) * 2 + 1] =
+			make_uint4(fbits(b.x - t0.x), fbits(b.y - t0.y), fbits(c.x - t0.x), fbits(c.y - t0.y));
+	}
 	uint32_t inst_flags_id = (flags & 0xffffu) | (uint32_t(inst) << 16);
 	const lucid_config& cfg = p.cfg;
 	F3 origin = xyz4(cfg.frustum.ws_origin0);

@@ -24,11 +24,16 @@ def _dptr(t):
     return None if t is None else ctypes.c_void_p(t.data_ptr())
 
 
+def _dptr_or_none(t):
+    return None if t is None else t.data_ptr()
+
+
 class FrameInputs:
     """Device-resident inputs of one frame (RenderContext, src/lucid_base.h:72-84)."""
 
     def __init__(self, positions, colors, color_format, quads, instances, instance_colors, config,
-                 tri_opacity=None, num_verts=None):
+                 tri_opacity=None, num_verts=None, tex_coords=None, uv_rects=None, normals=None,
+                 opaque_tex=None, trans_tex=None):
         self.positions = positions
         self.colors = colors
         self.color_format = int(color_format)
@@ -38,6 +43,11 @@ class FrameInputs:
         self.tri_opacity = tri_opacity
         self.config = config  # scenes.LucidConfig (host)
         self.num_verts = int(num_verts if num_verts is not None else positions.shape[0])
+        self.tex_coords, self.uv_rects, self.normals = tex_coords, uv_rects, normals
+        # textures: (texels tensor, width, height, levels); descriptors live as long as the frame
+        self.opaque_tex, self.trans_tex = opaque_tex, trans_tex
+        self._tex_desc = [None if t is None else _lib.TextureC(t[0].data_ptr(), t[1], t[2], t[3], 0)
+                          for t in (opaque_tex, trans_tex)]
 
     @classmethod
     def from_scene(cls, scene, device="cuda", tri_opacity=None, colors=None):
@@ -54,10 +64,24 @@ class FrameInputs:
         else:
             col_t = up(cols.astype(np.float32))
         opac = scene.tri_opacity if tri_opacity is None else tri_opacity
+
+        def tex(t):
+            if t is None:
+                return None
+            return (up(t.packed().view(np.int32)), t.width, t.height, len(t.levels))
+
+        tc = getattr(scene, "tex_coords", None)
+        uvr = getattr(scene, "uv_rects", None)
+        nrm = getattr(scene, "normals", None)
         return cls(up(scene.positions.astype(np.float32)), col_t, scene.color_format,
                    up(scene.quads.view(np.int32)), up(scene.instances.astype(np.int32)),
                    up(scene.instance_colors.view(np.int32)), scene.config,
-                   None if opac is None else up(np.asarray(opac, np.float32)))
+                   None if opac is None else up(np.asarray(opac, np.float32)),
+                   tex_coords=None if tc is None else up(np.asarray(tc, np.float32)),
+                   uv_rects=None if uvr is None else up(np.asarray(uvr, np.float32)),
+                   normals=None if nrm is None else up(np.asarray(nrm, np.uint32).view(np.int32)),
+                   opaque_tex=tex(getattr(scene, "opaque_tex", None)),
+                   trans_tex=tex(getattr(scene, "trans_tex", None)))
 
     def c_struct(self) -> _lib.FrameInputsC:
         return _lib.FrameInputsC(
@@ -67,7 +91,11 @@ class FrameInputs:
             num_instances=int(self.instances.shape[0]), instances=self.instances.data_ptr(),
             instance_colors=self.instance_colors.data_ptr() if self.instance_colors is not None else None,
             tri_opacity=self.tri_opacity.data_ptr() if self.tri_opacity is not None else None,
-            config=ctypes.addressof(self.config))
+            config=ctypes.addressof(self.config),
+            tex_coords=_dptr_or_none(self.tex_coords), instance_uv_rects=_dptr_or_none(self.uv_rects),
+            normals=_dptr_or_none(self.normals),
+            opaque_texture=None if self._tex_desc[0] is None else ctypes.addressof(self._tex_desc[0]),
+            transparent_texture=None if self._tex_desc[1] is None else ctypes.addressof(self._tex_desc[1]))
 
 
 def default_options() -> _lib.Options:

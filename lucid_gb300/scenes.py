@@ -29,6 +29,10 @@ import numpy as np
 
 # LUCID_INST_* flags (data/shaders/shared/definitions.glsl:85-94)
 INST_HAS_VERTEX_COLORS = 0x001
+INST_HAS_VERTEX_NORMALS = 0x004
+INST_TEX_OPAQUE = 0x010
+INST_HAS_UV_RECT = 0x020
+INST_HAS_ALBEDO_TEXTURE = 0x040
 INST_HAS_COLOR = 0x200
 
 COLOR_RGBA8 = 0
@@ -174,6 +178,53 @@ def build_instances(draw_calls, max_instances: int = 64 * 1024):
 
 
 @dataclass
+class Texture:
+    """RGBA8 texture with its mip chain: levels[l] is uint32 [max(1, h >> l), max(1, w >> l)]."""
+    levels: list
+
+    @property
+    def width(self):
+        return int(self.levels[0].shape[1])
+
+    @property
+    def height(self):
+        return int(self.levels[0].shape[0])
+
+    def packed(self) -> np.ndarray:
+        return np.concatenate([lv.reshape(-1) for lv in self.levels]).astype(np.uint32)
+
+
+def make_texture(width, height, seed=0, alpha_range=(1.0, 1.0), levels=None) -> Texture:
+    """Seeded RGBA8 texture (smooth colour waves plus noise) with a 2x2 box-filtered mip chain."""
+    rng = np.random.default_rng(seed)
+    yy, xx = np.meshgrid(np.arange(height), np.arange(width), indexing="ij")
+    base = np.stack([0.5 + 0.5 * np.sin(xx * (0.3 + 0.2 * rng.random()) + rng.random() * 6),
+                     0.5 + 0.5 * np.sin(yy * (0.25 + 0.2 * rng.random()) + rng.random() * 6),
+                     0.5 + 0.5 * np.sin((xx + yy) * 0.11 + rng.random() * 6)], -1)
+    base = np.clip(base + rng.normal(0, 0.05, base.shape), 0, 1)
+    alpha = rng.uniform(alpha_range[0], alpha_range[1], size=(height, width, 1))
+    img = np.concatenate([base, alpha], -1)
+    n = levels or (int(math.log2(max(width, height))) + 1)
+    out = []
+    cur = img
+    for _ in range(n):
+        q = np.clip(np.rint(cur * 255.0), 0, 255).astype(np.uint32)
+        out.append(q[..., 0] | (q[..., 1] << 8) | (q[..., 2] << 16) | (q[..., 3] << 24))
+        h, w = cur.shape[:2]
+        if h == 1 and w == 1:
+            break
+        nh, nw = max(1, h // 2), max(1, w // 2)
+        cur = cur[:nh * (h // nh), :nw * (w // nw)].reshape(nh, h // nh, nw, w // nw, 4).mean((1, 3))
+    return Texture(out)
+
+
+def encode_normals(n: np.ndarray) -> np.ndarray:
+    """10 bits per axis, v = round(n * 511 + 512) (the inverse of funcs.glsl:61-66)."""
+    q = np.clip(np.rint(n * 511.0 + 512.0), 0, 1023).astype(np.uint32)
+    return q[..., 0] | (q[..., 1] << 10) | (q[..., 2] << 20)
+
+
+@dataclass
 class Scene:
     width: int
     height: int
@@ -186,6 +237,12 @@ class Scene:
     config: LucidConfig
     tri_opacity: np.ndarray | None = None  # float32 [Q*2] or None
     meta: dict = field(default_factory=dict)
+    # optional shading inputs (shading.glsl:125-176)
+    tex_coords: np.ndarray | None = None   # float32 [V, 2]
+    uv_rects: np.ndarray | None = None     # float32 [N, 4]: uv min, uv size per instance
+    normals: np.ndarray | None = None      # uint32 [V] encoded normals
+    opaque_tex: "Texture | None" = None
+    trans_tex: "Texture | None" = None
 
     @property
     def num_quads(self) -> int:
@@ -306,6 +363,37 @@ def _grid_quads(nu, nv, base):
                     a = base + j * (nu + 1) + i
                     quads.append((a, a + 1, a + 1 + (nu + 1), a + (nu + 1)))
     return np.array(quads, dtype=np.uint32)
+
+
+def textured_scene(width=160, height=120, num_tris=800, seed=0, uv_rects=True, vertex_normals=True,
+                   opaque_fraction=0.5, tex_size=(64, 32), tri_opacity_range=None, color_format=COLOR_RGBA8):
+    """Random triangles with texture coordinates (spanning up to a few texture repeats), two
+    instance groups sampling the opaque and the transparent texture (optionally through per-instance
+    uv rects), optional per-vertex normals: the shading inputs of shading.glsl:125-176."""
+    sc = random_tris(width, height, num_tris, seed=seed, area_median=300.0, area_sigma=1.0,
+                     color_format=color_format, tri_opacity_range=tri_opacity_range)
+    rng = np.random.default_rng(seed + 1)
+    nv = sc.positions.shape[0]
+    tex = rng.uniform(-1.0, 3.0, size=(nv, 2)).astype(np.float32)
+    n_op = int(round(num_tris * opaque_fraction))
+    base = INST_HAS_VERTEX_COLORS | INST_HAS_ALBEDO_TEXTURE | (INST_HAS_VERTEX_NORMALS if vertex_normals else 0)
+    if uv_rects:
+        base |= INST_HAS_UV_RECT
+    dcs = [(0, n_op, base | INST_TEX_OPAQUE, 0xFFFFFFFF), (n_op, num_tris - n_op, base, 0xFFC0E0FF)]
+    instances, inst_colors, _ = build_instances([dc for dc in dcs if dc[1] > 0])
+    rects = np.zeros((instances.shape[0], 4), np.float32)
+    rects[:, :2] = rng.uniform(0.0, 0.5, size=(instances.shape[0], 2))
+    rects[:, 2:] = rng.uniform(0.25, 0.5, size=(instances.shape[0], 2))
+    normals = None
+    if vertex_normals:
+        nrm = rng.normal(size=(nv, 3))
+        nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+        normals = encode_normals(nrm)
+    ot = make_texture(tex_size[0], tex_size[1], seed=seed + 2)
+    tt = make_texture(tex_size[1], tex_size[0], seed=seed + 3, alpha_range=(0.2, 1.0))
+    return Scene(width, height, sc.positions, sc.colors, sc.color_format, sc.quads, instances, inst_colors,
+                 sc.config, sc.tri_opacity, dict(sc.meta, kind="textured"), tex_coords=tex,
+                 uv_rects=rects if uv_rects else None, normals=normals, opaque_tex=ot, trans_tex=tt)
 
 
 def tri_mesh(kind="sphere", nu=64, nv=32, seed=0, noise=0.01, shuffle=True):

@@ -26,6 +26,8 @@ class OracleInputs(ctypes.Structure):
         ("num_instances", ctypes.c_int32), ("instances", ctypes.c_void_p),
         ("instance_colors", ctypes.c_void_p), ("tri_opacity", ctypes.c_void_p),
         ("config", ctypes.c_void_p),
+        ("tex_coords", ctypes.c_void_p), ("instance_uv_rects", ctypes.c_void_p), ("normals", ctypes.c_void_p),
+        ("opaque_texture", ctypes.c_void_p), ("transparent_texture", ctypes.c_void_p),
         ("bin_subset", ctypes.c_void_p), ("num_bin_subset", ctypes.c_int32),
         ("num_threads", ctypes.c_int32),
     ]
@@ -68,6 +70,35 @@ def _ptr(a):
     return None if a is None else a.ctypes.data
 
 
+class _Texture(ctypes.Structure):
+    _fields_ = [("texels", ctypes.c_void_p), ("width", ctypes.c_int32), ("height", ctypes.c_int32),
+                ("num_levels", ctypes.c_int32), ("_pad", ctypes.c_int32)]
+
+
+def _shading_inputs(scene, keep):
+    """Pointers of the optional shading inputs (kept alive in `keep`)."""
+    def arr(a, dt):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(a, dt)
+        keep.append(a)
+        return a.ctypes.data
+
+    def tex(t):
+        if t is None:
+            return None
+        texels = t.packed()
+        desc = _Texture(texels.ctypes.data, t.width, t.height, len(t.levels), 0)
+        keep.extend([texels, desc])
+        return ctypes.addressof(desc)
+
+    return dict(tex_coords=arr(getattr(scene, "tex_coords", None), np.float32),
+                instance_uv_rects=arr(getattr(scene, "uv_rects", None), np.float32),
+                normals=arr(getattr(scene, "normals", None), np.uint32),
+                opaque_texture=tex(getattr(scene, "opaque_tex", None)),
+                transparent_texture=tex(getattr(scene, "trans_tex", None)))
+
+
 def run(scene, max_visible_quads: int | None = None, raster: bool = True, image64: bool = False,
         bin_subset=None, threads: int = 1, max_per_pixel: int = 0, flags: int = 0,
         low_high_threshold: int = 1024, setup_outputs: bool = True, order_mode: int = 0):
@@ -108,7 +139,9 @@ def run(scene, max_visible_quads: int | None = None, raster: bool = True, image6
             out["frag_prims"] = np.full((h, w, max_per_pixel), -1, np.int32)
 
     cfg = scene.config
+    keep = []
     ins = OracleInputs(
+        **_shading_inputs(scene, keep),
         width=w, height=h, max_visible_quads=mvq, low_high_threshold=low_high_threshold,
         flags=flags, order_mode=order_mode, positions=_ptr(positions), colors=_ptr(colors),
         color_format=scene.color_format, num_verts=positions.shape[0], quads_ib=_ptr(quads),
@@ -171,7 +204,9 @@ class GradModel:
             icol=np.ascontiguousarray(scene.instance_colors, np.uint32),
             opac=None if scene.tri_opacity is None else np.ascontiguousarray(scene.tri_opacity, np.float32))
         k = self._keep
+        self._shade_keep = []
         ins = OracleInputs(
+            **_shading_inputs(scene, self._shade_keep),
             width=scene.width, height=scene.height, max_visible_quads=mvq, low_high_threshold=1024,
             flags=0, order_mode=0, positions=_ptr(k["positions"]), colors=_ptr(k["colors"]),
             color_format=scene.color_format, num_verts=k["positions"].shape[0], quads_ib=_ptr(k["quads"]),

@@ -152,7 +152,7 @@ struct State {
 	int w, h, bcx, bcy, bins, mvq;
 	V3 origin, dir0, dirx, diry, ray_dir0;
 	// outputs of setup
-	std::vector<uint32_t> quad_aabbs, quad_source, quad_colors, quad_verts;
+	std::vector<uint32_t> quad_aabbs, quad_source, quad_colors, quad_verts, quad_normals, quad_tex;
 	std::vector<uint32_t> tri_bary, tri_scan, tri_depth, tri_normals;
 	std::vector<uint32_t> quad_inst; // instance id per quad slot
 	int nvis[2] = {0, 0};
@@ -394,6 +394,8 @@ void quadSetup(State& s, oracle_outputs* out) {
 	s.quad_source.assign(mvq, 0);
 	s.quad_colors.assign(size_t(mvq) * 4, 0);
 	s.quad_verts.assign(size_t(mvq) * 4, 0);
+	s.quad_normals.assign(size_t(mvq) * 4, 0);
+	s.quad_tex.assign(size_t(mvq) * 8, 0);
 	s.quad_inst.assign(mvq, 0);
 	s.tri_bary.assign(size_t(mvq) * 16, 0);
 	s.tri_scan.assign(size_t(mvq) * 16, 0);
@@ -430,11 +432,25 @@ void quadSetup(State& s, oracle_outputs* out) {
 			for(int k = 0; k < 4; k++)
 				s.quad_verts[size_t(slot) * 4 + k] = v[k];
 			uint32_t flags = id.flags;
-			// storeQuad (quad_setup.glsl:256-272): RGBA8 vertex colours
+			// storeQuad (quad_setup.glsl:256-272): RGBA8 vertex colours, vertex normals, texture
+			// coordinates relative to the first vertex
 			if((flags & LUCID_INST_HAS_VERTEX_COLORS) && in->color_format == LUCID_COLOR_RGBA8) {
 				const uint32_t* cols = (const uint32_t*)in->colors;
 				for(int k = 0; k < 4; k++)
 					s.quad_colors[size_t(slot) * 4 + k] = cols[v[k]];
+			}
+			if((flags & LUCID_INST_HAS_VERTEX_NORMALS) && in->normals)
+				for(int k = 0; k < 4; k++)
+					s.quad_normals[size_t(slot) * 4 + k] = in->normals[v[k]];
+			if((flags & LUCID_INST_HAS_ALBEDO_TEXTURE) && in->tex_coords) {
+				const float* tc = in->tex_coords;
+				const float t0x = tc[size_t(v[0]) * 2], t0y = tc[size_t(v[0]) * 2 + 1];
+				uint32_t* q = &s.quad_tex[size_t(slot) * 8];
+				q[0] = fbits(t0x), q[1] = fbits(t0y);
+				for(int k = 1; k < 4; k++) {
+					q[2 * k] = fbits(tc[size_t(v[k]) * 2] - t0x);
+					q[2 * k + 1] = fbits(tc[size_t(v[k]) * 2 + 1] - t0y);
+				}
 			}
 			uint32_t inst_flags_id = (flags & 0xffffu) | (uint32_t(inst) << 16);
 			for(int second = 0; second < 2; second++) {
@@ -637,46 +653,186 @@ struct Frag {
 	float depth;    // inv_ray_pos
 };
 
-void shadeFragment(const State& s, const Frag& f, int px, int py, float col[4]) {
+// log2(x) for finite x > 0: exponent plus the series 2 atanh(t) = ln(m), t = (m - 1) / (m + 1),
+// on the mantissa m in [sqrt(1/2), sqrt(2)) up to t^13; each operation rounds separately, as in
+// the CUDA path. 0 gives -inf, +inf gives +inf, negative or NaN input NaN.
+float seriesLog2(float x) {
+	if(x != x || x < 0.0f)
+		return NAN;
+	if(x == 0.0f)
+		return -INFINITY;
+	if(x == INFINITY)
+		return x;
+	int e = 0;
+	uint32_t b = fbits(x);
+	if(((b >> 23) & 0xffu) == 0u) {
+		x = x * 8388608.0f;
+		b = fbits(x);
+		e = -23;
+	}
+	e += int((b >> 23) & 0xffu) - 127;
+	float m = bitsf((b & 0x7fffffu) | 0x3f800000u);
+	if(m > 0x1.6a09e6p+0f) {
+		m = m * 0.5f;
+		e = e + 1;
+	}
+	const float t = (m - 1.0f) / (m + 1.0f);
+	const float t2 = t * t;
+	float sr = 0x1.3b13b2p-4f;      // 1/13
+	sr = sr * t2 + 0x1.745d18p-4f; // 1/11
+	sr = sr * t2 + 0x1.c71c72p-4f; // 1/9
+	sr = sr * t2 + 0x1.24924ap-3f; // 1/7
+	sr = sr * t2 + 0x1.99999ap-3f; // 1/5
+	sr = sr * t2 + 0x1.555556p-2f; // 1/3
+	sr = sr * t2 + 1.0f;
+	const float ln_m = (2.0f * t) * sr;
+	return float(e) + ln_m * 0x1.715476p+0f; // 1/ln 2
+}
+
+// Bilinear sample of one mip level (repeat addressing, texel centres at half integers).
+void texSampleLevel(const lucid_texture& t, int level, float u, float v, float out[4]) {
+	size_t off = 0;
+	for(int l = 0; l < level; l++)
+		off += size_t(std::max(1, t.width >> l)) * size_t(std::max(1, t.height >> l));
+	const int w = std::max(1, t.width >> level), h = std::max(1, t.height >> level);
+	u = u - floorf(u);
+	v = v - floorf(v);
+	if(u != u)
+		u = 0.0f;
+	if(v != v)
+		v = 0.0f;
+	const float fu = u * float(w) - 0.5f, fv = v * float(h) - 0.5f;
+	const float xf = floorf(fu), yf = floorf(fv);
+	const float a = fu - xf, b = fv - yf;
+	const int x0 = int(xf), y0 = int(yf);
+	auto texel = [&](int x, int y, float c[4]) {
+		x = x < 0 ? x + w : (x >= w ? x - w : x);
+		y = y < 0 ? y + h : (y >= h ? y - h : y);
+		decodeRGBA8(t.texels[off + size_t(y) * w + x], c);
+	};
+	float c00[4], c10[4], c01[4], c11[4];
+	texel(x0, y0, c00), texel(x0 + 1, y0, c10), texel(x0, y0 + 1, c01), texel(x0 + 1, y0 + 1, c11);
+	const float wa = (1.0f - a) * (1.0f - b), wb = a * (1.0f - b), wc = (1.0f - a) * b, wd = a * b;
+	for(int k = 0; k < 4; k++)
+		out[k] = ((c00[k] * wa + c10[k] * wb) + c01[k] * wc) + c11[k] * wd;
+}
+
+// textureGrad, trilinear and repeat-addressed (the reference's sampler adds 16x anisotropy,
+// src/lucid_base.h:30, the hardware's own footprint, not modelled)
+void texSampleGrad(const lucid_texture* t, float u, float v, float dxu, float dxv, float dyu, float dyv,
+				   float out[4]) {
+	if(!t || !t->texels) {
+		out[0] = out[1] = out[2] = out[3] = 1.0f;
+		return;
+	}
+	const float W = float(t->width), H = float(t->height);
+	const float ax = dxu * W, ay = dxv * H, bx = dyu * W, by = dyv * H;
+	const float rho = fmaxf(sqrtf(ax * ax + ay * ay), sqrtf(bx * bx + by * by));
+	float lambda = seriesLog2(rho);
+	if(!(lambda > 0.0f))
+		lambda = 0.0f;
+	lambda = fminf(lambda, float(t->num_levels - 1));
+	const float lf = floorf(lambda);
+	const int l0 = int(lf);
+	const float f = lambda - lf;
+	texSampleLevel(*t, l0, u, v, out);
+	if(f > 0.0f) {
+		float c1[4];
+		texSampleLevel(*t, l0 + 1, u, v, c1);
+		const float g = 1.0f - f;
+		for(int k = 0; k < 4; k++)
+			out[k] = out[k] * g + c1[k] * f;
+	}
+}
+
+// Everything shadeSample (shading.glsl:107-165) computes before lighting, in its float order.
+struct ShadeCoreO {
+	float col[4];    // colour with vertex colours and opacity
+	float factor[4]; // instance colour x texture colour
+	float b0, b1;
+	uint32_t flags, inst;
+};
+
+ShadeCoreO shadeCore(const State& s, const Frag& f, int px, int py) {
 	const oracle_inputs* in = s.in;
+	ShadeCoreO o;
 	const uint32_t* d = &s.tri_depth[size_t(f.tri) * 4];
 	const uint32_t* b = &s.tri_bary[size_t(f.tri) * 8];
-	float fx = float(px), fy = float(py);
-	float ray_pos = 1.0f / f.depth;
-	float e0 = bitsf(b[0]) * fx + (bitsf(b[1]) * fy + bitsf(b[2]));
-	float e1 = bitsf(b[4]) * fx + (bitsf(b[5]) * fy + bitsf(b[6]));
-	float b0 = e0 * ray_pos, b1 = e1 * ray_pos;
-	b0 = b0 - bitsf(b[3]);
-	b1 = b1 - bitsf(b[7]);
-	uint32_t flags = d[3] & 0xffffu, inst = d[3] >> 16;
+	const float fx = float(px), fy = float(py);
+	const float ray_pos = 1.0f / f.depth;
+	const float e0 = bitsf(b[0]) * fx + (bitsf(b[1]) * fy + bitsf(b[2]));
+	const float e1 = bitsf(b[4]) * fx + (bitsf(b[5]) * fy + bitsf(b[6]));
+	const float braw0 = e0 * ray_pos, braw1 = e1 * ray_pos;
+	const float b0 = braw0 - bitsf(b[3]);
+	const float b1 = braw1 - bitsf(b[7]);
+	o.b0 = b0, o.b1 = b1;
+	o.flags = d[3] & 0xffffu, o.inst = d[3] >> 16;
+	const uint32_t quad = f.tri >> 1, second = f.tri & 1;
+	float* col = o.col;
 	col[0] = col[1] = col[2] = col[3] = 1.0f;
-	if((flags & LUCID_INST_HAS_COLOR) && in->instance_colors)
-		decodeRGBA8(in->instance_colors[inst], col);
-	if(flags & LUCID_INST_HAS_VERTEX_COLORS) {
-		uint32_t quad = f.tri >> 1, second = f.tri & 1;
+	if((o.flags & LUCID_INST_HAS_COLOR) && in->instance_colors)
+		decodeRGBA8(in->instance_colors[o.inst], col);
+	if(o.flags & LUCID_INST_HAS_ALBEDO_TEXTURE) {
+		// shading.glsl:125-159: bary derivatives, texture coordinates, optional uv rect
+		const float ray_posx = 1.0f / (f.depth + bitsf(d[0]));
+		const float ray_posy = 1.0f / (f.depth + bitsf(d[1]));
+		const float bdx0 = (e0 + bitsf(b[0])) * ray_posx - braw0, bdx1 = (e1 + bitsf(b[4])) * ray_posx - braw1;
+		const float bdy0 = (e0 + bitsf(b[1])) * ray_posy - braw0, bdy1 = (e1 + bitsf(b[5])) * ray_posy - braw1;
+		const uint32_t* q = &s.quad_tex[size_t(quad) * 8];
+		const float t0x = bitsf(q[0]), t0y = bitsf(q[1]);
+		const float t1x = bitsf(second ? q[4] : q[2]), t1y = bitsf(second ? q[5] : q[3]);
+		const float t2x = bitsf(second ? q[6] : q[4]), t2y = bitsf(second ? q[7] : q[5]);
+		float u = b0 * t1x + (b1 * t2x + t0x), v = b0 * t1y + (b1 * t2y + t0y);
+		float dxu = bdx0 * t1x + bdx1 * t2x, dxv = bdx0 * t1y + bdx1 * t2y;
+		float dyu = bdy0 * t1x + bdy1 * t2x, dyv = bdy0 * t1y + bdy1 * t2y;
+		if((o.flags & LUCID_INST_HAS_UV_RECT) && in->instance_uv_rects) {
+			const float* r = in->instance_uv_rects + size_t(o.inst) * 4;
+			u = r[2] * (u - floorf(u)) + r[0];
+			v = r[3] * (v - floorf(v)) + r[1];
+			dxu = dxu * r[2], dxv = dxv * r[3], dyu = dyu * r[2], dyv = dyv * r[3];
+		}
+		float tc[4];
+		if(o.flags & LUCID_INST_TEX_OPAQUE) {
+			texSampleGrad(in->opaque_texture, u, v, dxu, dxv, dyu, dyv, tc);
+			tc[3] = 1.0f;
+		} else {
+			texSampleGrad(in->transparent_texture, u, v, dxu, dxv, dyu, dyv, tc);
+		}
+		for(int k = 0; k < 4; k++)
+			col[k] = col[k] * tc[k];
+	}
+	for(int k = 0; k < 4; k++)
+		o.factor[k] = col[k];
+	if(o.flags & LUCID_INST_HAS_VERTEX_COLORS) {
 		float c[3][4];
-		uint32_t vid[3] = {s.quad_verts[size_t(quad) * 4 + 0],
-						   s.quad_verts[size_t(quad) * 4 + 1 + second],
+		uint32_t vid[3] = {s.quad_verts[size_t(quad) * 4 + 0], s.quad_verts[size_t(quad) * 4 + 1 + second],
 						   s.quad_verts[size_t(quad) * 4 + 2 + second]};
 		for(int k = 0; k < 3; k++) {
 			if(in->color_format == LUCID_COLOR_RGBA8) {
 				decodeRGBA8(((const uint32_t*)in->colors)[vid[k]], c[k]);
 			} else if(in->color_format == LUCID_COLOR_RGBA16F) {
-				const uint16_t* h = (const uint16_t*)in->colors + size_t(vid[k]) * 4;
+				const uint16_t* hh = (const uint16_t*)in->colors + size_t(vid[k]) * 4;
 				for(int j = 0; j < 4; j++)
-					c[k][j] = halfToFloat(h[j]);
+					c[k][j] = halfToFloat(hh[j]);
 			} else {
 				const float* fc = (const float*)in->colors + size_t(vid[k]) * 4;
 				for(int j = 0; j < 4; j++)
 					c[k][j] = fc[j];
 			}
 		}
-		float wgt = (1.0f - b0) - b1;
+		const float wgt = (1.0f - b0) - b1;
 		for(int j = 0; j < 4; j++)
 			col[j] = col[j] * (wgt * c[0][j] + (b0 * c[1][j] + b1 * c[2][j]));
 	}
 	if(in->tri_opacity)
 		col[3] = col[3] * in->tri_opacity[f.prim];
+	return o;
+}
+
+void shadeFragment(const State& s, const Frag& f, int px, int py, float col[4]) {
+	const ShadeCoreO o = shadeCore(s, f, px, py);
+	for(int k = 0; k < 4; k++)
+		col[k] = o.col[k];
 }
 
 // Fragments of every pixel of one bin (row-major 32x32 lists, unsorted); returns the count of
@@ -836,30 +992,7 @@ float refPow(float x, float y) {
 		return x == 0.0f ? 0.0f : NAN;
 	if(x == INFINITY)
 		return y > 0.0f ? INFINITY : 0.0f;
-	int e = 0;
-	uint32_t b = fbits(x);
-	if(((b >> 23) & 0xffu) == 0u) { // subnormal
-		x = x * 8388608.0f;
-		b = fbits(x);
-		e = -23;
-	}
-	e += int((b >> 23) & 0xffu) - 127;
-	float m = bitsf((b & 0x7fffffu) | 0x3f800000u);
-	if(m > 0x1.6a09e6p+0f) {
-		m = m * 0.5f;
-		e = e + 1;
-	}
-	const float t = (m - 1.0f) / (m + 1.0f);
-	const float t2 = t * t;
-	float sr = 0x1.3b13b2p-4f;      // 1/13
-	sr = sr * t2 + 0x1.745d18p-4f; // 1/11
-	sr = sr * t2 + 0x1.c71c72p-4f; // 1/9
-	sr = sr * t2 + 0x1.24924ap-3f; // 1/7
-	sr = sr * t2 + 0x1.99999ap-3f; // 1/5
-	sr = sr * t2 + 0x1.555556p-2f; // 1/3
-	sr = sr * t2 + 1.0f;
-	const float ln_m = (2.0f * t) * sr;
-	const float l2 = float(e) + ln_m * 0x1.715476p+0f; // 1/ln 2
+	const float l2 = seriesLog2(x);
 	const float z = y * l2;
 	if(z >= 128.0f)
 		return INFINITY;
@@ -907,12 +1040,24 @@ uint32_t shadeRef(const State& s, uint32_t tri, uint32_t prim, int px, int py, f
 	const uint32_t* d = &s.tri_depth[size_t(tri) * 4];
 	const float inv_ray_pos = bitsf(d[0]) * float(px) + (bitsf(d[1]) * float(py) + bitsf(d[2]));
 	depth = inv_ray_pos;
-	float c[4];
-	shadeFragment(s, Frag{0u, prim, tri, inv_ray_pos}, px, py, c);
+	const ShadeCoreO sc = shadeCore(s, Frag{0u, prim, tri, inv_ray_pos}, px, py);
+	float c[4] = {sc.col[0], sc.col[1], sc.col[2], sc.col[3]};
 	if(c[3] == 0.0f)
 		return 0u;
 	const lucid_lighting& L = s.in->config->lighting;
-	const V3 n = decodeNormalUint(s.tri_normals[tri]);
+	V3 n;
+	if((sc.flags & LUCID_INST_HAS_VERTEX_NORMALS) && s.in->normals) {
+		// shading.glsl:168-174: normals interpolated with the perspective-correct barycentrics
+		const uint32_t* qn = &s.quad_normals[size_t(tri >> 1) * 4];
+		const uint32_t second = tri & 1;
+		const V3 n0 = decodeNormalUint(qn[0]);
+		const V3 n1 = sub(decodeNormalUint(qn[1 + second]), n0);
+		const V3 n2 = sub(decodeNormalUint(qn[2 + second]), n0);
+		n = v3(sc.b0 * n1.x + (sc.b1 * n2.x + n0.x), sc.b0 * n1.y + (sc.b1 * n2.y + n0.y),
+			   sc.b0 * n1.z + (sc.b1 * n2.z + n0.z));
+	} else {
+		n = decodeNormalUint(s.tri_normals[tri]);
+	}
 	const float dn = (-L.sun_dir[0]) * n.x + (-L.sun_dir[1]) * n.y + (-L.sun_dir[2]) * n.z;
 	const float light = fmaxf(0.0f, dn * 0x1.666666p-1f + 0x1.333334p-2f); // * 0.7 + 0.3
 	for(int ch = 0; ch < 3; ch++) {
@@ -1456,11 +1601,11 @@ extern "C" void* oracle_grad_build(const oracle_inputs* in) {
 				gf.vid[2] = s.quad_verts[size_t(quad) * 4 + 2 + second];
 				gf.prim = f.prim;
 				gf.wgt[0] = wgt, gf.wgt[1] = b0, gf.wgt[2] = b1;
-				float ic[4] = {1.0f, 1.0f, 1.0f, 1.0f};
-				if((flags & LUCID_INST_HAS_COLOR) && in->instance_colors)
-					decodeRGBA8(in->instance_colors[inst], ic);
+				// instance colour x texture colour: the factor of the vertex colours
+				const ShadeCoreO core = shadeCore(s, f, pxx, py);
+				(void)inst;
 				for(int ch = 0; ch < 4; ch++)
-					gf.inst[ch] = ic[ch];
+					gf.inst[ch] = core.factor[ch];
 				gf.has_vc = (flags & LUCID_INST_HAS_VERTEX_COLORS) != 0;
 				out.push_back(gf);
 			}

@@ -43,6 +43,12 @@ typedef struct oracle_inputs {
 	const uint32_t* instance_colors;
 	const float* tri_opacity;
 	const lucid_config* config;
+	/* optional shading inputs as in lucid_frame_inputs (host memory; texture texels too) */
+	const float* tex_coords;
+	const float* instance_uv_rects;
+	const uint32_t* normals;
+	const lucid_texture* opaque_texture;
+	const lucid_texture* transparent_texture;
 	/* raster only these bins (ascending bin ids); NULL = all bins */
 	const int32_t* bin_subset;
 	int32_t num_bin_subset;

@@ -192,3 +192,49 @@ def test_fp64_gradient_model_analytic_vs_fd(oracle):
     scale = np.abs(dvc).max()
     assert np.abs(bvc - dvc).max() <= 1e-5 * scale
     assert np.abs(bop - dop).max() <= 1e-5 * np.abs(dop).max()
+
+
+def _textured_quad_scene(W=16, H=8, x0=10, y0=6, z=4.0, opaque=True, uv_rect=None, levels=None):
+    """One screen-aligned quad (two tris) covering W x H pixels from (x0, y0) at constant depth
+    with uv (0,0)..(1,1) at its corners: pixel centres land on texel centres of level 0."""
+    tris = [[(x0, y0, z), (x0 + W, y0, z), (x0 + W, y0 + H, z)], [(x0, y0, z), (x0 + W, y0 + H, z), (x0, y0 + H, z)]]
+    cols = [[(255, 255, 255, 255)] * 3] * 2
+    sc = scenes.screen_triangles(tris, cols, 48, 32)
+    uv = np.array([[0, 0], [1, 0], [1, 1], [0, 0], [1, 1], [0, 1]], np.float32)
+    flags = scenes.INST_HAS_ALBEDO_TEXTURE | (scenes.INST_TEX_OPAQUE if opaque else 0)
+    if uv_rect is not None:
+        flags |= scenes.INST_HAS_UV_RECT
+    inst, icol, _ = scenes.build_instances([(0, 2, flags, 0xFFFFFFFF)])
+    tex = scenes.make_texture(W, H, seed=3, alpha_range=(0.3, 0.9), levels=levels)
+    sc = scenes.Scene(**{**sc.__dict__, "instances": inst, "instance_colors": icol, "tex_coords": uv,
+                         "uv_rects": None if uv_rect is None else np.array([uv_rect], np.float32),
+                         "opaque_tex": tex if opaque else None, "trans_tex": None if opaque else tex})
+    return sc, tex
+
+
+def test_texture_kat_texel_centres(oracle):
+    """Pixel centres on texel centres, one texel per pixel: the image is the texture (level 0,
+    no blending between texels)."""
+    W, H, x0, y0 = 16, 8, 10, 6
+    sc, tex = _textured_quad_scene(W, H, x0, y0)
+    img = oracle.run(sc)["image"]
+    lv0 = tex.levels[0]
+    want = np.stack([(lv0 >> (8 * k)) & 0xFF for k in range(3)], -1).astype(np.float32) / np.float32(255)
+    np.testing.assert_allclose(img[y0:y0 + H, x0:x0 + W, :3], want, atol=2e-6)
+
+
+def test_texture_transparent_and_uv_rect(oracle):
+    """Transparent texture: alpha from the texture; a uv rect maps the quad onto a sub-rectangle
+    (fract, then scale and offset, shading.glsl:146-150)."""
+    W, H, x0, y0 = 16, 8, 10, 6
+    sc, tex = _textured_quad_scene(W, H, x0, y0, opaque=False)
+    img = oracle.run(sc)["image"]
+    lv0 = tex.levels[0].astype(np.int64)
+    rgba = np.stack([(lv0 >> (8 * k)) & 0xFF for k in range(4)], -1).astype(np.float64) / 255.0
+    want = rgba[..., :3] * rgba[..., 3:]  # black background
+    np.testing.assert_allclose(img[y0:y0 + H, x0:x0 + W, :3], want, atol=2e-5)
+    # a uv rect of the left half: pixel x samples u = 0.5 * (x + 0.5) / W
+    sc2, tex2 = _textured_quad_scene(W, H, x0, y0, uv_rect=(0.0, 0.0, 0.5, 1.0))
+    img2 = oracle.run(sc2)["image"]
+    assert np.abs(img2[y0:y0 + H, x0:x0 + W] - img[y0:y0 + H, x0:x0 + W]).max() > 1e-3
+    assert np.isfinite(img2).all()
