@@ -223,7 +223,9 @@ typedef struct lucid_options {
 	int32_t grad_store_fragments; /* fragment store of lucid_render_forward_grad: 0 = grows on
 	                               * demand, > 0 = fixed capacity, < 0 = none (the backward pass
 	                               * recomputes the fragment lists instead of reading them)      */
-	int32_t reserved[4];
+	int32_t slab_fragments;    /* raster: fragments per unfinished pixel a depth slab aims at
+	                            * (0 = 264; a large value counts every key at once)            */
+	int32_t reserved[3];
 } lucid_options;
 
 /* ---------------------------------------------------------------------------------------- */

@@ -46,6 +46,7 @@ struct FrameParams {
 	int max_bin_refs;
 	int band_capacity;
 	int low_high_threshold;
+	int slab_target;      // fragments per unfinished pixel a depth slab aims at
 	int num_setup_ctas;
 	int num_binning_ctas;
 	uint32_t flags;

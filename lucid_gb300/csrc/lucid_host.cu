@@ -181,6 +181,9 @@ void setShadingInputs(FrameParams& p, const lucid_frame_inputs* in) {
 	p.trans_tex = in->transparent_texture ? *in->transparent_texture : lucid_texture{};
 }
 
+// fragments per unfinished pixel that a depth slab of the raster aims at
+int slabTarget(const lucid_renderer* r) { return r->opts.slab_fragments > 0 ? r->opts.slab_fragments : 264; }
+
 FrameParams makeParams(lucid_renderer* r, const lucid_frame_inputs* in, float* out) {
 	FrameParams p{};
 	p.positions = in->positions;
@@ -202,6 +205,7 @@ FrameParams makeParams(lucid_renderer* r, const lucid_frame_inputs* in, float* o
 	p.max_bin_refs = r->opts.max_bin_refs;
 	p.band_capacity = r->opts.band_capacity;
 	p.low_high_threshold = r->opts.low_high_threshold;
+	p.slab_target = slabTarget(r);
 	p.num_setup_ctas = (in->num_quads + kSetupThreads - 1) / kSetupThreads;
 	p.num_binning_ctas = r->opts.binning_ctas;
 	p.flags = r->opts.flags;
@@ -592,6 +596,7 @@ static lucid_status rasterImpl(lucid_renderer* r, const lucid_frame_inputs* in, 
 		return st;
 	r->grad_ready = false;
 	FrameParams p = r->last;
+	p.slab_target = slabTarget(r);
 	p.colors = in->colors;
 	p.color_format = in->color_format;
 	p.instance_colors = in->instance_colors;
@@ -1030,6 +1035,7 @@ void batchParams(lucid_renderer* r, BatchPlan* b, const lucid_view* views, std::
 		p.max_bin_refs = r->opts.max_bin_refs;
 		p.band_capacity = r->opts.band_capacity;
 		p.low_high_threshold = r->opts.low_high_threshold;
+		p.slab_target = slabTarget(r);
 		p.num_setup_ctas = viewSetupCtas(nq);
 		p.num_binning_ctas = b->binning_ctas[size_t(v)];
 		p.flags = r->opts.flags & ~uint32_t(LUCID_OPT_TIMERS);

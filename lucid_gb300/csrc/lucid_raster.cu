@@ -42,6 +42,9 @@ constexpr int kStage = 4096;        // shaded fragments per shading round (64 KB
 constexpr int kWindow = 176;        // target fragments per pixel per depth window
 constexpr int kGroupBudget = 6144;  // sum over a group's pixels of min(count, kWindow)
 constexpr int kHistWords = 8192;    // per-group depth histogram (pixels x buckets)
+constexpr int kCoarseShift = 20;    // fragment estimate bins: depth keys >> 20 (4096 bins)
+constexpr int kCoarseBins = 1 << (32 - kCoarseShift);
+constexpr int kMaxSlabs = 64;       // depth slabs of one group at most
 
 struct RasterSmem {
 	// kv[b][0] = keys, kv[b][1] = payloads of buffer b; the buffer not holding the sorted
@@ -75,6 +78,10 @@ struct RasterSmem {
 	unsigned long long stat_hbt;
 	unsigned long long store_base; // kRasterStore: first store slot of the bin
 	uint32_t kmin, kmax;
+	uint32_t group_frags;      // fragments of the current group's pixels
+	uint32_t slab_lo, slab_hi; // depth slab whose keys the histogram holds
+	int slab_next;             // index of the next slab
+	int slab_first[kMaxSlabs]; // first estimate bin of every slab (INT_MAX: no such slab)
 	int bin;
 	int group_end;
 	int single_digit;
@@ -86,6 +93,12 @@ struct RasterSmem {
 };
 
 static_assert(sizeof(RasterSmem) <= 227 * 1024, "raster shared memory exceeds one SM");
+
+// Depth histogram slot of pixel t's bucket bk (2^nb_log >= 32 buckets per pixel). The bucket is
+// XOR-swizzled by the pixel's lane so that the 32 pixels of a row, which mostly hit the same
+// bucket of a planar triangle, fall into 32 different shared-memory banks.
+__device__ __forceinline__ int histIdx(int t, int bk, int nb_log) { return (t << nb_log) | (bk ^ (t & 31)); }
+static_assert(kCoarseBins <= kHistWords, "the fragment estimate lives in the depth histogram");
 
 size_t rasterSmemBytes() { return sizeof(RasterSmem); }
 int rasterThreads() { return RT; }
@@ -294,12 +307,13 @@ __device__ void writePixel(const FrameParams& p, int px, int py, float4 c) {
 // With `ekeys` (the entries' depth-key ranges over the group, written by the histogram pass)
 // only entries whose range meets the current window of some pixel of the row are visited; the
 // window of pixel t holds the keys of its buckets [px_lo, px_cut] (bucket = (key - kmin) >> shift).
+// With `ekeys` and flo <= fhi, entries are culled against the fixed key range [flo, fhi] instead.
 template <typename Fn>
 __device__ __forceinline__ void forEachGroupFragment(const FrameParams& p, const RasterSmem& s,
 													  const uint2* scratch, int band_cap, int bin_x,
 													  int bin_y, int p0, int p1, Fn fn,
 													  const uint2* ekeys = nullptr, uint32_t kmin = 0u,
-													  int shift = 0) {
+													  int shift = 0, uint32_t flo = 1u, uint32_t fhi = 0u) {
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	const int r0 = p0 >> 5, r1 = (p1 - 1) >> 5;
 	const int nrows = r1 - r0 + 1;
@@ -315,7 +329,9 @@ __device__ __forceinline__ void forEachGroupFragment(const FrameParams& p, const
 	const int t = pix - p0;
 	const float fx = float(bin_x + lane), fy = float(bin_y + row);
 	uint32_t wlo = 0u, whi = 0xffffffffu;
-	if(ekeys) {
+	if(ekeys && flo <= fhi) {
+		wlo = flo, whi = fhi;
+	} else if(ekeys) {
 		uint32_t lo_k = 0xffffffffu, hi_k = 0u;
 		if(in_group && s.px_cut[t] >= 0) {
 			const unsigned long long a = (unsigned long long)kmin + ((unsigned long long)s.px_lo[t] << shift);
@@ -655,6 +671,7 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 				s.group_end = lo;
 				s.kmin = 0xffffffffu;
 				s.kmax = 0u;
+				s.group_frags = 0u;
 			}
 			__syncthreads();
 			const int p1 = s.group_end;
@@ -664,6 +681,14 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 			double acc64[3] = {0.0, 0.0, 0.0}, c64[3] = {0.0, 0.0, 0.0}, T64 = 1.0;
 			float grad[3] = {0.0f, 0.0f, 0.0f};
 			bool heavy = false;
+			{
+				uint32_t c = t < npix ? uint32_t(s.pix_count[p0 + t]) : 0u;
+#pragma unroll
+				for(int o = 16; o > 0; o >>= 1)
+					c += __shfl_xor_sync(0xffffffffu, c, o);
+				if(lane == 0 && c)
+					atomicAdd(&s.group_frags, c);
+			}
 			if(t < npix) {
 				int c = s.pix_count[p0 + t];
 				heavy = c > kWindow;
@@ -694,10 +719,21 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 			}
 			const bool windowed = __syncthreads_or(heavy);
 
-			// C1. key range and per-pixel depth histograms of a heavy group
+			// C1. key range, fragment estimate and per-pixel depth histograms of a heavy group
 			int nb_log = 0, shift = 0;
 			if(windowed) {
 				const int r0 = p0 >> 5, r1 = (p1 - 1) >> 5;
+				// slabs only when the group holds more than two slabs' fragments (a second pass over
+				// the entries costs more than it saves on shallower groups)
+				const int n_active0 = __syncthreads_count(t < npix && s.px_state[t] != 1);
+				const bool slabs = (unsigned long long)s.group_frags >
+								   2ull * (unsigned long long)max(1, p.slab_target) * (unsigned long long)max(1, n_active0);
+				if(slabs)
+					for(int i = tid; i < kCoarseBins; i += RT)
+						s.hist[i] = 0u;
+				if(tid < kMaxSlabs)
+					s.slab_first[tid] = 0x7fffffff;
+				__syncthreads();
 				uint32_t kmn = 0xffffffffu, kmx = 0u;
 				for(int b = r0 >> 2; b <= (r1 >> 2); b++) {
 					const int ne = s.band_count[b];
@@ -706,6 +742,7 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 						uint4 d = __ldg(p.tri_depth + entryTri(e));
 						float dx = bitsf(d.x), dy = bitsf(d.y), dz = bitsf(d.z);
 						uint32_t emn = 0xffffffffu, emx = 0u;
+						int wsum = 0;
 #pragma unroll
 						for(int r = 0; r < 4; r++) {
 							int row = b * 4 + r;
@@ -715,6 +752,7 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 							int xlo = max(lo, p0 - 32 * row), xhi = min(hi, p1 - 1 - 32 * row);
 							if(xlo > xhi)
 								continue;
+							wsum += xhi - xlo + 1;
 							// the evaluation is monotone in x, so the row's extremes are its ends
 							float ty = dy * float(bin_y + row) + dz;
 							uint32_t ka = nearFirstKey(dx * float(bin_x + xlo) + ty);
@@ -724,6 +762,11 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 						}
 						kmn = min(kmn, emn);
 						kmx = max(kmx, emx);
+						// fragment estimate: the entry's covered pixels at the midpoint of its keys
+						if(slabs && wsum > 0) {
+							const uint32_t mid = (emn >> 1) + (emx >> 1) + (emn & emx & 1u);
+							atomicAdd(&s.hist[mid >> kCoarseShift], uint32_t(wsum));
+						}
 						// the entry's key range over the group, for the windows' entry culling;
 						// planes that could evaluate to NaN somewhere keep the full range
 						const float lim = 1e30f;
@@ -742,21 +785,85 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 					atomicMax(&s.kmax, kmx);
 				}
 				nb_log = 31 - __clz(max(1, min(256, kHistWords / npix))); // buckets per pixel = 2^nb_log
+				// slabs of about p.slab_target fragments per unfinished pixel: slab k starts at the
+				// first estimate bin whose preceding fragments reach k times that (the bins'
+				// exclusive prefix sum, 8 bins per thread)
+				__syncthreads();
+				if(slabs) {
+					constexpr int per = kCoarseBins / RT;
+					uint32_t v[per], sum = 0u;
+#pragma unroll
+					for(int k = 0; k < per; k++) {
+						v[k] = s.hist[tid * per + k];
+						sum += v[k];
+					}
+					uint32_t acc = blockExclusiveScan(sum, s.scan_tmpu, (uint32_t*)nullptr);
+					const unsigned long long slab_size =
+						(unsigned long long)max(1, p.slab_target) * (unsigned long long)max(1, n_active0);
+					const int bin_lo = int(s.kmin >> kCoarseShift), bin_hi = int(s.kmax >> kCoarseShift);
+#pragma unroll
+					for(int k = 0; k < per; k++) {
+						const int bin = tid * per + k;
+						if(bin >= bin_lo && bin <= bin_hi) {
+							const int id = bin == bin_lo ? 0 : int(min(acc / slab_size, (unsigned long long)(kMaxSlabs - 1)));
+							atomicMin(&s.slab_first[id], bin);
+						}
+						acc += v[k];
+					}
+				}
+				__syncthreads();
+			}
+			const int nbuckets = 1 << nb_log;
+			// Depth slabs: the histogram holds the keys of one slab [slab_lo, slab_hi] of the
+			// group's key range, sized by the coarse estimate for about p.slab_target fragments per
+			// unfinished pixel; the next slab is counted only when an unfinished pixel has used up
+			// the current one. Pixels whose transmittance reaches 0 early never pay for the keys
+			// behind them.
+			uint32_t slab_lo = 0u, slab_hi = 0xffffffffu;
+			auto buildSlab = [&](int slab) {
+				if(tid == 0) {
+					// the slab's keys: from its first bin (the group's kmin for slab 0) to the key
+					// before the next slab's first bin (the group's kmax for the last)
+					int next = slab + 1;
+					while(next < kMaxSlabs && s.slab_first[next] == 0x7fffffff)
+						next++;
+					s.slab_lo = slab == 0 ? s.kmin : uint32_t(s.slab_first[slab]) << kCoarseShift;
+					s.slab_hi = next >= kMaxSlabs ? s.kmax : (uint32_t(s.slab_first[next]) << kCoarseShift) - 1u;
+					s.slab_next = next;
+				}
 				for(int i = tid; i < (npix << nb_log); i += RT)
 					s.hist[i] = 0;
 				__syncthreads();
-				const uint32_t kmin = s.kmin;
-				uint32_t range = s.kmax - kmin;
-				int bits = range ? 32 - __clz(range) : 0;
+				slab_lo = s.slab_lo, slab_hi = s.slab_hi;
+				const uint32_t range = slab_hi - slab_lo;
+				const int bits = range ? 32 - __clz(range) : 0;
 				shift = max(0, bits - nb_log);
-				forEachGroupFragment(p, s, scratch, band_cap, bin_x, bin_y, p0, p1,
-									 [&](int tp, uint32_t key, int, int) {
-										 atomicAdd(&s.hist[(tp << nb_log) + int((key - kmin) >> shift)], 1u);
-									 });
+				const uint32_t lo_k = slab_lo, hi_k = slab_hi;
+				const int sh = shift;
+				// entries are culled against the slab only when it is narrower than the group's keys
+				const bool cull = lo_k > s.kmin || hi_k < s.kmax;
+				if(cull)
+					forEachGroupFragment(p, s, scratch, band_cap, bin_x, bin_y, p0, p1,
+										 [&](int tp, uint32_t key, int, int) {
+											 if(key >= lo_k && key <= hi_k)
+												 atomicAdd(&s.hist[histIdx(tp, int((key - lo_k) >> sh), nb_log)], 1u);
+										 },
+										 ekeys, 0u, 0, lo_k, hi_k);
+				else // the whole key range: no test per fragment
+					forEachGroupFragment(p, s, scratch, band_cap, bin_x, bin_y, p0, p1,
+										 [&](int tp, uint32_t key, int, int) {
+											 atomicAdd(&s.hist[histIdx(tp, int((key - lo_k) >> sh), nb_log)], 1u);
+										 });
 				__syncthreads();
-			}
+				if(t < npix && s.px_state[t] != 1) {
+					s.px_state[t] = 0;
+					s.px_lo[t] = 0;
+				}
+				__syncthreads();
+			};
+			if(windowed)
+				buildSlab(0);
 			RASTER_TIMER(2);
-			const int nbuckets = 1 << nb_log;
 			// fragments shaded per pixel per round: fewer pixels, deeper batches
 			const int batch = min(256, max(16, kStage / max(npix, 1)));
 
@@ -767,13 +874,15 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 				if(t < npix && s.px_state[t] == 0) {
 					if(windowed) {
 						int c = s.px_lo[t];
-						int acc = s.hist[(t << nb_log) + c];
+						int acc = s.hist[histIdx(t, c, nb_log)];
 						while(acc < kWindow && c + 1 < nbuckets) {
 							c++;
-							acc += s.hist[(t << nb_log) + c];
+							acc += s.hist[histIdx(t, c, nb_log)];
 						}
 						s.px_cut[t] = c;
 						wcount = acc;
+						if(acc == 0) // nothing left in this slab: wait for the next one, or done
+							s.px_state[t] = (s.px_done[t] < s.pix_count[p0 + t] && s.slab_hi < s.kmax) ? 2 : 1;
 					} else {
 						s.px_cut[t] = 0;
 						wcount = s.pix_count[p0 + t];
@@ -815,8 +924,8 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 					} else if(windowed) {
 						int off = wbase;
 						for(int b = s.px_lo[t]; b <= s.px_cut[t]; b++) {
-							int c = int(s.hist[(t << nb_log) + b]);
-							s.hist[(t << nb_log) + b] = uint32_t(off);
+							int c = int(s.hist[histIdx(t, b, nb_log)]);
+							s.hist[histIdx(t, b, nb_log)] = uint32_t(off);
 							off += c;
 							nsmall += c >= 2 && c <= 16;
 							nlarge += c > 16 && c <= 256;
@@ -841,8 +950,8 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 					if(windowed) {
 						const int lo = s.px_lo[t], cut = s.px_cut[t];
 						for(int b = lo; b <= cut; b++) {
-							int beg = int(s.hist[(t << nb_log) + b]);
-							int end = b < cut ? int(s.hist[(t << nb_log) + b + 1]) : wend;
+							int beg = int(s.hist[histIdx(t, b, nb_log)]);
+							int end = b < cut ? int(s.hist[histIdx(t, b + 1, nb_log)]) : wend;
 							add(beg, end - beg);
 						}
 					} else {
@@ -854,23 +963,29 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 					s.n_large = large_off;
 				}
 				const bool any_big = __syncthreads_or(big);
-				if(!__syncthreads_or(wcount > 0))
+				if(!__syncthreads_or(wcount > 0)) {
+					if(windowed && __syncthreads_or(t < npix && s.px_state[t] == 2)) {
+						buildSlab(s.slab_next); // a waiting pixel implies slab_hi < kmax
+						continue;
+					}
 					break;
+				}
 				const int n = total;
 
 				// C3. window fragments into their sub-segments
 				{
-					const uint32_t kmin = s.kmin;
 					forEachGroupFragment(p, s, scratch, band_cap, bin_x, bin_y, p0, p1,
 										 [&](int tp, uint32_t key, int b, int j) {
 											 if(s.px_cut[tp] < 0)
 												 return;
 											 int pos;
 											 if(windowed) {
-												 int bk = int((key - kmin) >> shift);
+												 if(key < slab_lo || key > slab_hi)
+													 return;
+												 int bk = int((key - slab_lo) >> shift);
 												 if(bk < s.px_lo[tp] || bk > s.px_cut[tp])
 													 return;
-												 pos = int(atomicAdd(&s.hist[(tp << nb_log) + bk], 1u));
+												 pos = int(atomicAdd(&s.hist[histIdx(tp, bk, nb_log)], 1u));
 											 } else {
 												 pos = atomicAdd(&s.px_wend[tp], 1);
 											 }
@@ -879,13 +994,13 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 												 s.kv[0][1][pos] = uint32_t(tp) | (uint32_t(b) << 8) | (uint32_t(j) << 11);
 											 }
 										 },
-										 windowed ? ekeys : nullptr, kmin, shift);
+										 windowed ? ekeys : nullptr, slab_lo, shift);
 				}
 				__syncthreads();
 				// every window segment must be exactly full (histogram and generation evaluate the
 				// same keys); anything else is an internal error
 				if(t < npix && s.px_cut[t] >= 0) {
-					int filled = windowed ? int(s.hist[(t << nb_log) + s.px_cut[t]]) : s.px_wend[t];
+					int filled = windowed ? int(s.hist[histIdx(t, s.px_cut[t], nb_log)]) : s.px_wend[t];
 					int want = s.px_wbase[t] + s.px_wcnt[t];
 					if(filled != want)
 						raiseError(p.info, LUCID_ERR_BIN_COUNT, uint32_t(bin), uint32_t(p0 + t),
@@ -1114,8 +1229,10 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 					s.px_done[t] += s.px_wcnt[t];
 					int next = s.px_cut[t] + 1;
 					s.px_lo[t] = next;
-					if(!windowed || next >= nbuckets)
+					if(!windowed)
 						s.px_state[t] = 1;
+					else if(next >= nbuckets) // the slab is used up: wait for the next one, or done
+						s.px_state[t] = (s.px_done[t] < s.pix_count[p0 + t] && slab_hi < s.kmax) ? 2 : 1;
 				}
 				__syncthreads();
 			}

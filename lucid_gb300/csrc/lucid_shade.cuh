@@ -164,11 +164,12 @@ __device__ __forceinline__ ShadeCore shadeCore(const FrameParams& p, uint32_t tr
 		col = make_float4(col.x * tc.x, col.y * tc.y, col.z * tc.z, col.w * tc.w);
 	}
 	s.factor = col;
-	const uint4 qv = __ldg(p.quad_verts + quad);
-	s.vid[0] = qv.x, s.vid[1] = second ? qv.z : qv.y, s.vid[2] = second ? qv.w : qv.z;
 	const float w = (1.0f - b0) - b1;
 	s.wgt = w;
+	s.vid[0] = s.vid[1] = s.vid[2] = 0u; // only read with vertex colours
 	if(s.flags & LUCID_INST_HAS_VERTEX_COLORS) {
+		const uint4 qv = __ldg(p.quad_verts + quad);
+		s.vid[0] = qv.x, s.vid[1] = second ? qv.z : qv.y, s.vid[2] = second ? qv.w : qv.z;
 		float4 c0, c1, c2;
 		if(p.color_format == LUCID_COLOR_RGBA8) {
 			const uint4 qc = __ldg(p.quad_colors + quad);

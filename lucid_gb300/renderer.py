@@ -112,7 +112,7 @@ class LucidRenderer:
                  max_visible_quads: int | None = None, max_bin_refs: int | None = None,
                  band_capacity: int | None = None, flags: int = 0, low_high_threshold: int = 1024,
                  raster_ctas_per_sm: int = 0, binning_ctas: int = 0, max_views: int = 1,
-                 grad_store_fragments: int = 0):
+                 grad_store_fragments: int = 0, slab_fragments: int = 0):
         if not torch.cuda.is_available():
             raise RuntimeError("lucid_gb300 needs a CUDA device")
         self.lib = _lib.load()
@@ -131,6 +131,7 @@ class LucidRenderer:
         o.binning_ctas = int(binning_ctas)
         o.max_views = int(max_views)
         o.grad_store_fragments = int(grad_store_fragments)
+        o.slab_fragments = int(slab_fragments)
         self.options = o
         self.width, self.height = int(width), int(height)
         self.bin_count_x = (self.width + 31) // 32

@@ -153,6 +153,22 @@ def test_depth_windows_concentrated_depths(gpu, oracle):
     compare(sc, oracle)
 
 
+@pytest.mark.parametrize("slab", [8, 64, 264, 1 << 30])
+def test_depth_slabs(gpu, oracle, slab):
+    """The per-pixel depth histograms built one key slab at a time (small slabs force many
+    slabs per group, a huge one counts every key at once): same fragment lists and image."""
+    from lucid_gb300.renderer import LucidRenderer
+    sc = scenes.random_tris(96, 64, 6000, seed=14, area_median=1500.0, area_sigma=0.4,
+                            alpha_range=(0.05, 0.5))
+    for dump in (512, 0):
+        r = LucidRenderer(sc.width, sc.height, max_input_quads=max(1024, sc.num_quads),
+                          max_visible_quads=max(1024, sc.num_quads),
+                          max_bin_refs=max(1 << 16, 8 * sc.num_quads), slab_fragments=slab)
+        g, o = compare(sc, oracle, dump=dump, renderer=r)
+        assert o["max_pixel_fragments"] > 400
+        r.close()
+
+
 def test_large_triangles_and_high_bins(gpu, oracle):
     sc = scenes.random_tris(200, 140, 3000, seed=4, area_median=2000.0, area_sigma=1.0,
                             large_fraction=0.05, large_area=(5000.0, 20000.0))
