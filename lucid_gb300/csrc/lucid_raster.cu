@@ -865,24 +865,46 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 				buildSlab(0);
 			RASTER_TIMER(2);
 			// fragments shaded per pixel per round: fewer pixels, deeper batches
-			const int batch = min(256, max(16, kStage / max(npix, 1)));
+			// (odd, so that the pixels' staging rows start in different shared-memory banks)
+			const int batch = (min(256, kStage / max(npix, 1)) - 1) | 1;
 
 			// C2. windows
 			while(true) {
-				// this round's window of every active pixel
+				// this round's window of every active pixel: in a heavy group one warp per pixel
+				// walks its buckets 32 at a time to the first cut holding >= kWindow fragments
+				if(windowed) {
+					for(int tp = warp; tp < npix; tp += NW) {
+						if(s.px_state[tp] != 0)
+							continue;
+						int acc = 0, cut = nbuckets - 1;
+						for(int c0 = s.px_lo[tp]; c0 < nbuckets; c0 += 32) {
+							const int bk = c0 + lane;
+							const int v = bk < nbuckets ? int(s.hist[histIdx(tp, bk, nb_log)]) : 0;
+							const int incl = warpInclusiveScan(v);
+							const uint32_t hit = __ballot_sync(0xffffffffu, bk < nbuckets && acc + incl >= kWindow);
+							if(hit) {
+								const int l = __ffs(hit) - 1;
+								cut = c0 + l;
+								acc += __shfl_sync(0xffffffffu, incl, l);
+								break;
+							}
+							acc += __shfl_sync(0xffffffffu, incl, 31);
+						}
+						if(lane == 0) {
+							s.px_cut[tp] = cut;
+							s.px_wcnt[tp] = acc;
+							if(acc == 0) // nothing left in this slab: wait for the next one, or done
+								s.px_state[tp] = (s.px_done[tp] < s.pix_count[p0 + tp] && s.slab_hi < s.kmax) ? 2 : 1;
+						}
+					}
+				}
+				if(tid == 0)
+					s.n_small = 0, s.n_large = 0;
+				__syncthreads();
 				int wcount = 0;
 				if(t < npix && s.px_state[t] == 0) {
 					if(windowed) {
-						int c = s.px_lo[t];
-						int acc = s.hist[histIdx(t, c, nb_log)];
-						while(acc < kWindow && c + 1 < nbuckets) {
-							c++;
-							acc += s.hist[histIdx(t, c, nb_log)];
-						}
-						s.px_cut[t] = c;
-						wcount = acc;
-						if(acc == 0) // nothing left in this slab: wait for the next one, or done
-							s.px_state[t] = (s.px_done[t] < s.pix_count[p0 + t] && s.slab_hi < s.kmax) ? 2 : 1;
+						wcount = s.px_wcnt[t];
 					} else {
 						s.px_cut[t] = 0;
 						wcount = s.pix_count[p0 + t];
@@ -910,57 +932,57 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 					}
 					wbase = blockExclusiveScan(wcount, s.scan_tmp, &total);
 				}
-				// sub-segments: one per pixel (light group) or one per bucket of the window; the
-				// bucket counts of the window become the sub-segment cursors
-				int nsmall = 0, nlarge = 0;
+				// sub-segments that need sorting: one per pixel (light group) or one per bucket of
+				// the window (the bucket counts of the window become the sub-segment cursors);
+				// list slots come from warp-aggregated counters
+				auto addSegments = [&](bool in, int beg, int c) {
+					const bool sm = in && c >= 2 && c <= 16, lg = in && c > 16 && c <= 256;
+					const uint32_t ms = __ballot_sync(0xffffffffu, sm), ml = __ballot_sync(0xffffffffu, lg);
+					int bs = 0, bl = 0;
+					if(lane == 0) {
+						if(ms)
+							bs = atomicAdd(&s.n_small, __popc(ms));
+						if(ml)
+							bl = atomicAdd(&s.n_large, __popc(ml));
+					}
+					bs = __shfl_sync(0xffffffffu, bs, 0);
+					bl = __shfl_sync(0xffffffffu, bl, 0);
+					if(sm)
+						s.sub_small[bs + __popc(ms & laneMaskLt())] = (uint32_t(beg) << 16) | uint32_t(c);
+					if(lg)
+						s.sub_large[bl + __popc(ml & laneMaskLt())] = (uint32_t(beg) << 16) | uint32_t(c);
+					return in && c > 256;
+				};
 				bool big = false;
 				if(t < npix) {
 					s.px_wbase[t] = wbase;
 					s.px_wend[t] = wbase;
 					s.px_bcur[t] = wbase;
 					s.px_wcnt[t] = wcount;
-					if(wcount == 0) {
+					if(wcount == 0)
 						s.px_cut[t] = -1; // not in this window (finished, empty or deferred)
-					} else if(windowed) {
-						int off = wbase;
-						for(int b = s.px_lo[t]; b <= s.px_cut[t]; b++) {
-							int c = int(s.hist[histIdx(t, b, nb_log)]);
-							s.hist[histIdx(t, b, nb_log)] = uint32_t(off);
-							off += c;
-							nsmall += c >= 2 && c <= 16;
-							nlarge += c > 16 && c <= 256;
-							big |= c > 256;
-						}
-					} else {
-						nsmall += wcount >= 2 && wcount <= 16;
-						nlarge += wcount > 16 && wcount <= 256;
-						big |= wcount > 256;
-					}
 				}
-				int small_off = blockExclusiveScan(nsmall, s.scan_tmp, (int*)nullptr);
-				int large_off = blockExclusiveScan(nlarge, s.scan_tmp, (int*)nullptr);
-				if(t < npix && (nsmall | nlarge)) {
-					const int wend = wbase + wcount;
-					auto add = [&](int beg, int c) {
-						if(c >= 2 && c <= 16)
-							s.sub_small[small_off++] = (uint32_t(beg) << 16) | uint32_t(c);
-						else if(c > 16 && c <= 256)
-							s.sub_large[large_off++] = (uint32_t(beg) << 16) | uint32_t(c);
-					};
-					if(windowed) {
-						const int lo = s.px_lo[t], cut = s.px_cut[t];
-						for(int b = lo; b <= cut; b++) {
-							int beg = int(s.hist[histIdx(t, b, nb_log)]);
-							int end = b < cut ? int(s.hist[histIdx(t, b + 1, nb_log)]) : wend;
-							add(beg, end - beg);
+				if(windowed) {
+					__syncthreads();
+					for(int tp = warp; tp < npix; tp += NW) {
+						const int cut = s.px_cut[tp];
+						if(cut < 0)
+							continue;
+						int off = s.px_wbase[tp];
+						for(int c0 = s.px_lo[tp]; c0 <= cut; c0 += 32) {
+							const int bk = c0 + lane;
+							const bool in = bk <= cut;
+							const int v = in ? int(s.hist[histIdx(tp, bk, nb_log)]) : 0;
+							const int incl = warpInclusiveScan(v);
+							const int beg = off + incl - v;
+							if(in)
+								s.hist[histIdx(tp, bk, nb_log)] = uint32_t(beg);
+							off += __shfl_sync(0xffffffffu, incl, 31);
+							big |= addSegments(in, beg, v);
 						}
-					} else {
-						add(wbase, wcount);
 					}
-				}
-				if(t == npix - 1) { // the last pixel's cursors end at the list totals
-					s.n_small = small_off;
-					s.n_large = large_off;
+				} else {
+					big = addSegments(t < npix && wcount > 0, wbase, wcount);
 				}
 				const bool any_big = __syncthreads_or(big);
 				if(!__syncthreads_or(wcount > 0)) {
@@ -1119,8 +1141,13 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 								uint32_t band = (v >> 8) & 7u, eslot = v >> 11;
 								uint32_t tri = entryTri(scratch[size_t(band) * band_cap + eslot]);
 								int pl = p0 + int(v & 0xffu);
-								stage[slot] = shadeFragment(p, tri, keyToDepth(K[f]), bin_x + (pl & 31),
-															bin_y + (pl >> 5));
+								float4 c = shadeFragment(p, tri, keyToDepth(K[f]), bin_x + (pl & 31),
+														 bin_y + (pl >> 5));
+								// the forward blend needs only the premultiplied colour and 1 - alpha:
+								// computed here in parallel, the same FP32 operations as in the blend
+								if constexpr(MODE == kRasterForward)
+									c = make_float4(c.x * c.w, c.y * c.w, c.z * c.w, 1.0f - c.w);
+								stage[slot] = c;
 							}
 						}
 					}
@@ -1133,6 +1160,38 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 						float T = s.px_T[t];
 						float c0 = s.px_c[t][0], c1 = s.px_c[t][1], c2 = s.px_c[t][2];
 						bool finished = false;
+						if(MODE == kRasterForward && !dump && !additive && !alpha_threshold) {
+							// the plain forward blend without a branch per fragment: once T is 0 the
+							// remaining steps of a run of 8 add -0 (the identity of FP32 addition)
+							// and keep T, so the colour is that of the front-to-back loop that stops
+							// at T == 0 (the same FP32 operations in the same order). A finished
+							// pixel's cursor is not read again.
+							const float4* sp = stage + t * batch;
+							const int n = min(batch, fend - f);
+							auto step = [&](float4 q) {
+								const bool on = T != 0.0f;
+								c0 = c0 + (on ? q.x * T : -0.0f);
+								c1 = c1 + (on ? q.y * T : -0.0f);
+								c2 = c2 + (on ? q.z * T : -0.0f);
+								T = T * (on ? q.w : 1.0f);
+							};
+							int j = 0;
+							for(; j + 8 <= n; j += 8) {
+								float4 q[8];
+#pragma unroll
+								for(int u = 0; u < 8; u++)
+									q[u] = sp[j + u];
+#pragma unroll
+								for(int u = 0; u < 8; u++)
+									step(q[u]);
+								if(T == 0.0f)
+									break;
+							}
+							for(; T != 0.0f && j < n; j++)
+								step(sp[j]);
+							finished = T == 0.0f;
+							f += j;
+						} else
 						for(int j = 0; j < batch && f < fend; j++, f++) {
 							float4 c;
 							if constexpr(MODE == kRasterBackward) {
@@ -1195,7 +1254,24 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 											int(fragPrim(p, scratch, band_cap, V[f]));
 								}
 							}
-							if(additive) {
+							if constexpr(MODE == kRasterForward) {
+								// c = (premultiplied rgb, 1 - alpha)
+								if(additive) {
+									c0 = c0 + c.x;
+									c1 = c1 + c.y;
+									c2 = c2 + c.z;
+								} else {
+									c0 = c0 + c.x * T;
+									c1 = c1 + c.y * T;
+									c2 = c2 + c.z * T;
+									T = T * c.w;
+									if((T == 0.0f && !dump) || (alpha_threshold && T < (1.0f / 128.0f))) {
+										finished = true;
+										f++;
+										break;
+									}
+								}
+							} else if(additive) {
 								c0 = c0 + c.x * c.w;
 								c1 = c1 + c.y * c.w;
 								c2 = c2 + c.z * c.w;
