@@ -105,10 +105,13 @@ int rasterThreads() { return RT; }
 
 __device__ __forceinline__ uint32_t entryTri(uint2 e) { return (e.x >> 20) | ((e.y >> 20) << 12); }
 
-__device__ __forceinline__ uint32_t fragPrim(const FrameParams& p, const uint2* scratch, int band_cap,
-											 uint32_t val) {
-	uint32_t band = (val >> 8) & 7u, slot = val >> 11;
-	uint32_t tri = entryTri(scratch[size_t(band) * band_cap + slot]);
+// A window fragment's payload: pixel of the group (8 bits) and tri (24 bits, the band entries'
+// tri field).
+__device__ __forceinline__ uint32_t fragPayload(int tp, uint32_t tri) { return uint32_t(tp) | (tri << 8); }
+__device__ __forceinline__ uint32_t payloadTri(uint32_t val) { return val >> 8; }
+
+__device__ __forceinline__ uint32_t fragPrim(const FrameParams& p, uint32_t val) {
+	const uint32_t tri = payloadTri(val);
 	return __ldg(p.quad_source + (tri >> 1)) * 2 + (tri & 1);
 }
 
@@ -298,7 +301,7 @@ __device__ void writePixel(const FrameParams& p, int px, int py, float4 c) {
 		reinterpret_cast<float4*>(p.out_rgba)[size_t(py) * p.width + px] = c;
 }
 
-// Visits every fragment of pixels [p0, p1) of the bin: fn(t, key, band, slot) with t the pixel
+// Visits every fragment of pixels [p0, p1) of the bin: fn(t, key, tri) with t the pixel
 // index inside the group, called by the lane owning pixel t. Warps are assigned to the group's
 // rows (lane = pixel column) and split a row's band entries; entries are loaded 32 at a time
 // (one per lane) and broadcast by shuffle. The key is evaluated exactly as in the oracle
@@ -375,7 +378,7 @@ __device__ __forceinline__ void forEachGroupFragment(const FrameParams& p, const
 			if(covered) {
 				float ty = kdy * fy + kdz;
 				float inv_ray_pos = kdx * fx + ty;
-				fn(t, nearFirstKey(inv_ray_pos), b, j0 + k);
+				fn(t, nearFirstKey(inv_ray_pos), (ex >> 20) | ((ey >> 20) << 12));
 			}
 		}
 	}
@@ -844,14 +847,14 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 				const bool cull = lo_k > s.kmin || hi_k < s.kmax;
 				if(cull)
 					forEachGroupFragment(p, s, scratch, band_cap, bin_x, bin_y, p0, p1,
-										 [&](int tp, uint32_t key, int, int) {
+										 [&](int tp, uint32_t key, uint32_t) {
 											 if(key >= lo_k && key <= hi_k)
 												 atomicAdd(&s.hist[histIdx(tp, int((key - lo_k) >> sh), nb_log)], 1u);
 										 },
 										 ekeys, 0u, 0, lo_k, hi_k);
 				else // the whole key range: no test per fragment
 					forEachGroupFragment(p, s, scratch, band_cap, bin_x, bin_y, p0, p1,
-										 [&](int tp, uint32_t key, int, int) {
+										 [&](int tp, uint32_t key, uint32_t) {
 											 atomicAdd(&s.hist[histIdx(tp, int((key - lo_k) >> sh), nb_log)], 1u);
 										 });
 				__syncthreads();
@@ -997,7 +1000,7 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 				// C3. window fragments into their sub-segments
 				{
 					forEachGroupFragment(p, s, scratch, band_cap, bin_x, bin_y, p0, p1,
-										 [&](int tp, uint32_t key, int b, int j) {
+										 [&](int tp, uint32_t key, uint32_t tri) {
 											 if(s.px_cut[tp] < 0)
 												 return;
 											 int pos;
@@ -1013,7 +1016,7 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 											 }
 											 if(pos < s.px_wbase[tp] + s.px_wcnt[tp]) {
 												 s.kv[0][0][pos] = key;
-												 s.kv[0][1][pos] = uint32_t(tp) | (uint32_t(b) << 8) | (uint32_t(j) << 11);
+												 s.kv[0][1][pos] = fragPayload(tp, tri);
 											 }
 										 },
 										 windowed ? ekeys : nullptr, slab_lo, shift);
@@ -1092,9 +1095,9 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 						while(e < n && K[e] == K[i] && ((V[e] ^ V[i]) & 0xffu) == 0)
 							e++;
 						for(int a = i + 1; a < e; a++) {
-							uint32_t va = V[a], pa = fragPrim(p, scratch, band_cap, va);
+							uint32_t va = V[a], pa = fragPrim(p, va);
 							int c = a - 1;
-							while(c >= i && fragPrim(p, scratch, band_cap, V[c]) > pa) {
+							while(c >= i && fragPrim(p, V[c]) > pa) {
 								V[c + 1] = V[c];
 								c--;
 							}
@@ -1120,11 +1123,8 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 							const uint32_t dst = p.grad_px_off[size_t(py) * p.width + px] + uint32_t(s.px_done[tp]);
 							const int wb = s.px_wbase[tp], wc = s.px_wcnt[tp];
 							for(int k = lane; k < wc; k += 32) {
-								uint32_t v = V[wb + k];
-								uint32_t band = (v >> 8) & 7u, eslot = v >> 11;
-								p.grad_tris[dst + k] = eslot < uint32_t(band_cap)
-														   ? entryTri(scratch[size_t(band) * band_cap + eslot])
-														   : 0xffffffffu;
+								const uint32_t tri = payloadTri(V[wb + k]);
+								p.grad_tris[dst + k] = tri < 2u * uint32_t(p.max_visible_quads) ? tri : 0xffffffffu;
 							}
 						}
 					}
@@ -1138,8 +1138,7 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 							int f = s.px_bcur[tp] + j;
 							if(f < s.px_wend[tp] && s.px_state[tp] == 0) {
 								uint32_t v = V[f];
-								uint32_t band = (v >> 8) & 7u, eslot = v >> 11;
-								uint32_t tri = entryTri(scratch[size_t(band) * band_cap + eslot]);
+								uint32_t tri = payloadTri(v);
 								int pl = p0 + int(v & 0xffu);
 								float4 c = shadeFragment(p, tri, keyToDepth(K[f]), bin_x + (pl & 31),
 														 bin_y + (pl >> 5));
@@ -1198,9 +1197,7 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 								// recompute the fragment's shading and route dL/dC to its inputs:
 								// dC/dc = a*T, dC/da = c*T - S/(1-a) with S the colour behind it,
 								// S = C - (colour accumulated up to and including it) in FP64
-								uint32_t v = V[f];
-								uint32_t band = (v >> 8) & 7u, eslot = v >> 11;
-								uint32_t tri = entryTri(scratch[size_t(band) * band_cap + eslot]);
+								uint32_t tri = payloadTri(V[f]);
 								int pl = p0 + t;
 								FragmentShade fs = shadeFragmentFull(p, tri, keyToDepth(K[f]),
 																	 bin_x + (pl & 31), bin_y + (pl >> 5));
@@ -1251,7 +1248,7 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 									int px = bin_x + (pl & 31), py = bin_y + (pl >> 5);
 									if(px < p.width && py < p.height)
 										p.dump_prims[(size_t(py) * p.width + px) * p.dump_max + idx] =
-											int(fragPrim(p, scratch, band_cap, V[f]));
+											int(fragPrim(p, V[f]));
 								}
 							}
 							if constexpr(MODE == kRasterForward) {
