@@ -1132,9 +1132,12 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 				}
 				while(MODE != kRasterStore) {
 					if constexpr(MODE != kRasterBackward) {
+						// slot / batch by multiply and shift (exact for odd batch in [15, 255] and
+						// slot < 4096)
+						const uint32_t bmul = (1u << 20) / uint32_t(batch) + 1u;
 #pragma unroll 2
 						for(int slot = tid; slot < npix * batch; slot += RT) {
-							int tp = slot / batch, j = slot - tp * batch;
+							int tp = int((uint32_t(slot) * bmul) >> 20), j = slot - tp * batch;
 							int f = s.px_bcur[tp] + j;
 							if(f < s.px_wend[tp] && s.px_state[tp] == 0) {
 								uint32_t v = V[f];
