@@ -351,34 +351,41 @@ __device__ __forceinline__ void forEachGroupFragment(const FrameParams& p, const
 			return; // no pixel of this row takes part in the window
 		wlo = lo_k, whi = hi_k;
 	}
+	// the group's columns in this row
+	const int glo = max(0, p0 - 32 * row), ghi = min(31, p1 - 1 - 32 * row);
 	for(int j0 = jbeg; j0 < jend; j0 += 32) {
+		// lane j's entry: its span in this row, its tri and the row's part of its plane
+		// (dy * py + dz, the same for every pixel of the row); only entries whose span meets
+		// the group's columns take part
 		const int j = j0 + lane;
-		uint2 e = make_uint2(0x1fu << 5 * 3, 0u); // empty spans for lanes past the end
-		float dx = 0.0f, dy = 0.0f, dz = 0.0f;
 		bool rel = j < jend;
 		if(rel && ekeys) {
 			const uint2 kr = ekeys[size_t(b) * band_cap + j];
 			rel = kr.y >= wlo && kr.x <= whi;
 		}
+		uint32_t span = 0u, tri = 0u;
+		float dx = 0.0f, ty = 0.0f;
 		if(rel) {
-			e = scratch[size_t(b) * band_cap + j];
-			uint4 d = __ldg(p.tri_depth + entryTri(e));
-			dx = bitsf(d.x), dy = bitsf(d.y), dz = bitsf(d.z);
+			const uint2 e = scratch[size_t(b) * band_cap + j];
+			const int lo = (e.x >> rshift) & 31, hi = (e.y >> rshift) & 31;
+			rel = max(lo, glo) <= min(hi, ghi);
+			if(rel) {
+				tri = entryTri(e);
+				const uint4 d = __ldg(p.tri_depth + tri);
+				dx = bitsf(d.x);
+				ty = bitsf(d.y) * fy + bitsf(d.z);
+				span = uint32_t(lo) | uint32_t(hi) << 5;
+			}
 		}
 		for(uint32_t todo = __ballot_sync(0xffffffffu, rel); todo != 0u; todo &= todo - 1u) {
 			const int k = __ffs(todo) - 1;
-			uint32_t ex = __shfl_sync(0xffffffffu, e.x, k), ey = __shfl_sync(0xffffffffu, e.y, k);
-			int lo = (ex >> rshift) & 31, hi = (ey >> rshift) & 31;
-			bool covered = in_group && lane >= lo && lane <= hi;
-			if(!__any_sync(0xffffffffu, covered))
-				continue;
-			float kdx = __shfl_sync(0xffffffffu, dx, k);
-			float kdy = __shfl_sync(0xffffffffu, dy, k);
-			float kdz = __shfl_sync(0xffffffffu, dz, k);
-			if(covered) {
-				float ty = kdy * fy + kdz;
-				float inv_ray_pos = kdx * fx + ty;
-				fn(t, nearFirstKey(inv_ray_pos), (ex >> 20) | ((ey >> 20) << 12));
+			const uint32_t sp = __shfl_sync(0xffffffffu, span, k);
+			const float kdx = __shfl_sync(0xffffffffu, dx, k), kty = __shfl_sync(0xffffffffu, ty, k);
+			const uint32_t ktri = __shfl_sync(0xffffffffu, tri, k);
+			const int lo = int(sp & 31u), hi = int(sp >> 5);
+			if(in_group && lane >= lo && lane <= hi) {
+				const float inv_ray_pos = kdx * fx + kty;
+				fn(t, nearFirstKey(inv_ray_pos), ktri);
 			}
 		}
 	}
