@@ -68,10 +68,13 @@ struct RasterSmem {
 	int px_done[kGroupPixels];   // fragments already processed (verification dump index)
 	int px_state[kGroupPixels];  // 0 active, 1 finished
 	// sub-segments of the current window that need sorting, as (start << 16 | count):
-	// counts 2..16 are sorted by one thread, 17..256 by one warp
+	// counts 2..16 are sorted by one thread, by size class (2, 3-4, 5-8, 9-16; class 0 from the
+	// front and class 2 from the back of sub_small, classes 1 and 3 likewise in `radix`, which
+	// the window does not need unless it is radix sorted), 17..256 by one warp
 	uint32_t sub_small[kGroupCap / 2];
 	uint32_t sub_large[kGroupCap / 17 + 1];
-	int n_small, n_large;
+	unsigned long long n_cls; // counts of the four size classes, 16 bits each
+	int n_large;
 	int band_count[8];
 	int scan_tmp[NW + 1];
 	uint32_t scan_tmpu[NW + 1];
@@ -93,11 +96,20 @@ struct RasterSmem {
 };
 
 static_assert(sizeof(RasterSmem) <= 227 * 1024, "raster shared memory exceeds one SM");
+static_assert(256 * NW == kGroupCap / 2, "the small sub-segment lists share the radix histograms' size");
 
 // Depth histogram slot of pixel t's bucket bk (2^nb_log >= 32 buckets per pixel). The bucket is
 // XOR-swizzled by the pixel's lane so that the 32 pixels of a row, which mostly hit the same
 // bucket of a planar triangle, fall into 32 different shared-memory banks.
 __device__ __forceinline__ int histIdx(int t, int bk, int nb_log) { return (t << nb_log) | (bk ^ (t & 31)); }
+
+// A sub-segment of a window to sort: start relative to its pixel's window (13 bits), count
+// (9 bits) and pixel of the group (8 bits).
+__device__ __forceinline__ uint32_t segEntry(int rel, int cnt, int tp) {
+	return uint32_t(rel) | uint32_t(cnt) << 13 | uint32_t(tp) << 22;
+}
+__device__ __forceinline__ int segCount(uint32_t e) { return int((e >> 13) & 0x1ffu); }
+__device__ __forceinline__ int segPixel(uint32_t e) { return int(e >> 22); }
 static_assert(kCoarseBins <= kHistWords, "the fragment estimate lives in the depth histogram");
 
 size_t rasterSmemBytes() { return sizeof(RasterSmem); }
@@ -682,6 +694,7 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 				s.kmin = 0xffffffffu;
 				s.kmax = 0u;
 				s.group_frags = 0u;
+				s.n_cls = 0ull, s.n_large = 0;
 			}
 			__syncthreads();
 			const int p1 = s.group_end;
@@ -880,8 +893,54 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 
 			// C2. windows
 			while(true) {
-				// this round's window of every active pixel: in a heavy group one warp per pixel
-				// walks its buckets 32 at a time to the first cut holding >= kWindow fragments
+				// this round's window of every active pixel and the window's sub-segments that need
+				// sorting: one per bucket of the window (heavy group) or one per pixel (light group).
+				// Positions are relative to the pixel's window start until the block scan places
+				// the windows: a heavy pixel's warp walks its buckets 32 at a time to the first cut
+				// holding >= kWindow fragments and turns the bucket counts into relative cursors.
+				// List slots come from warp-aggregated counters; an entry is
+				// (relative start, count, pixel), see segEntry.
+				auto addSegments = [&](bool in, int beg, int c, int tp) {
+					constexpr int kList = kGroupCap / 2;
+					const uint32_t entry = segEntry(beg, c, tp);
+					const int cls = c <= 2 ? 0 : c <= 4 ? 1 : c <= 8 ? 2 : 3;
+					const bool sm = in && c >= 2 && c <= 16, lg = in && c > 16 && c <= 256;
+					const uint32_t msm = __ballot_sync(0xffffffffu, sm), mlg = __ballot_sync(0xffffffffu, lg);
+					if(msm | mlg) {
+						const uint32_t b0 = __ballot_sync(0xffffffffu, cls & 1), b1 = __ballot_sync(0xffffffffu, cls & 2);
+						const uint32_t mc0 = msm & ~b0 & ~b1, mc1 = msm & b0 & ~b1, mc2 = msm & ~b0 & b1, mc3 = msm & b0 & b1;
+						unsigned long long base = 0ull;
+						int lbase = 0;
+						if(lane == 0) {
+							if(msm)
+								base = atomicAdd(&s.n_cls, (unsigned long long)__popc(mc0) |
+															   (unsigned long long)__popc(mc1) << 16 |
+															   (unsigned long long)__popc(mc2) << 32 |
+															   (unsigned long long)__popc(mc3) << 48);
+							if(mlg)
+								lbase = atomicAdd(&s.n_large, __popc(mlg));
+						}
+						base = __shfl_sync(0xffffffffu, base, 0);
+						lbase = __shfl_sync(0xffffffffu, lbase, 0);
+						const uint32_t lt = laneMaskLt();
+						if(sm) {
+							const uint32_t mine = cls == 0 ? mc0 : cls == 1 ? mc1 : cls == 2 ? mc2 : mc3;
+							const int pos = int((base >> (16 * cls)) & 0xffffu) + __popc(mine & lt);
+							if(cls == 0)
+								s.sub_small[pos] = entry;
+							else if(cls == 1)
+								s.radix[pos] = entry;
+							else if(cls == 2)
+								s.sub_small[kList - 1 - pos] = entry;
+							else
+								s.radix[kList - 1 - pos] = entry;
+						}
+						if(lg)
+							s.sub_large[lbase + __popc(mlg & lt)] = entry;
+					}
+					return in && c > 256;
+				};
+				bool big = false;
 				if(windowed) {
 					for(int tp = warp; tp < npix; tp += NW) {
 						if(s.px_state[tp] != 0)
@@ -892,13 +951,17 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 							const int v = bk < nbuckets ? int(s.hist[histIdx(tp, bk, nb_log)]) : 0;
 							const int incl = warpInclusiveScan(v);
 							const uint32_t hit = __ballot_sync(0xffffffffu, bk < nbuckets && acc + incl >= kWindow);
+							const int last = hit ? __ffs(hit) - 1 : 31;
+							const bool in = bk < nbuckets && lane <= last;
+							const int rel = acc + incl - v;
+							if(in)
+								s.hist[histIdx(tp, bk, nb_log)] = uint32_t(rel);
+							big |= addSegments(in, rel, v, tp);
+							acc += __shfl_sync(0xffffffffu, incl, last);
 							if(hit) {
-								const int l = __ffs(hit) - 1;
-								cut = c0 + l;
-								acc += __shfl_sync(0xffffffffu, incl, l);
+								cut = c0 + last;
 								break;
 							}
-							acc += __shfl_sync(0xffffffffu, incl, 31);
 						}
 						if(lane == 0) {
 							s.px_cut[tp] = cut;
@@ -907,24 +970,25 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 								s.px_state[tp] = (s.px_done[tp] < s.pix_count[p0 + tp] && s.slab_hi < s.kmax) ? 2 : 1;
 						}
 					}
-				}
-				if(tid == 0)
-					s.n_small = 0, s.n_large = 0;
-				__syncthreads();
-				int wcount = 0;
-				if(t < npix && s.px_state[t] == 0) {
-					if(windowed) {
-						wcount = s.px_wcnt[t];
-					} else {
+				} else {
+					const bool in = t < npix && s.px_state[t] == 0;
+					const int c = in ? s.pix_count[p0 + t] : 0;
+					if(in) {
 						s.px_cut[t] = 0;
-						wcount = s.pix_count[p0 + t];
+						s.px_wcnt[t] = c;
 					}
+					big = addSegments(in, 0, c, t);
 				}
+				__syncthreads();
+				int wcount = t < npix && s.px_state[t] == 0 ? s.px_wcnt[t] : 0;
 				int total;
 				int wbase = blockExclusiveScan(wcount, s.scan_tmp, &total);
-				if(total > kGroupCap) {
+				const bool over = total > kGroupCap;
+				bool deferred = false;
+				if(over) {
 					// defer the pixels that do not fit this round (their window stays)
 					bool fits = wbase + wcount <= kGroupCap;
+					deferred = !fits && wcount > 0;
 					if(!fits)
 						wcount = 0;
 					if(t < npix && s.px_state[t] == 0 && wbase == 0 && !fits) {
@@ -939,60 +1003,43 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 						s.px_state[t] = 1;
 						s.px_T[t] = 0.0f;
 						s.px_c[t][0] = 1.0f, s.px_c[t][1] = 0.0f, s.px_c[t][2] = 0.0f;
+						deferred = false;
 					}
 					wbase = blockExclusiveScan(wcount, s.scan_tmp, &total);
 				}
-				// sub-segments that need sorting: one per pixel (light group) or one per bucket of
-				// the window (the bucket counts of the window become the sub-segment cursors);
-				// list slots come from warp-aggregated counters
-				auto addSegments = [&](bool in, int beg, int c) {
-					const bool sm = in && c >= 2 && c <= 16, lg = in && c > 16 && c <= 256;
-					const uint32_t ms = __ballot_sync(0xffffffffu, sm), ml = __ballot_sync(0xffffffffu, lg);
-					int bs = 0, bl = 0;
-					if(lane == 0) {
-						if(ms)
-							bs = atomicAdd(&s.n_small, __popc(ms));
-						if(ml)
-							bl = atomicAdd(&s.n_large, __popc(ml));
-					}
-					bs = __shfl_sync(0xffffffffu, bs, 0);
-					bl = __shfl_sync(0xffffffffu, bl, 0);
-					if(sm)
-						s.sub_small[bs + __popc(ms & laneMaskLt())] = (uint32_t(beg) << 16) | uint32_t(c);
-					if(lg)
-						s.sub_large[bl + __popc(ml & laneMaskLt())] = (uint32_t(beg) << 16) | uint32_t(c);
-					return in && c > 256;
-				};
-				bool big = false;
 				if(t < npix) {
 					s.px_wbase[t] = wbase;
 					s.px_wend[t] = wbase;
 					s.px_bcur[t] = wbase;
-					s.px_wcnt[t] = wcount;
-					if(wcount == 0)
-						s.px_cut[t] = -1; // not in this window (finished, empty or deferred)
+					if(deferred) {
+						s.px_cut[t] = -2 - s.px_cut[t]; // keeps the cut for the restore below
+					} else {
+						s.px_wcnt[t] = wcount;
+						if(wcount == 0)
+							s.px_cut[t] = -1; // not in this window (finished, empty or deferred)
+					}
 				}
-				if(windowed) {
+				if(over && windowed) {
+					// a deferred heavy pixel gets its bucket counts back from the cursors
 					__syncthreads();
 					for(int tp = warp; tp < npix; tp += NW) {
-						const int cut = s.px_cut[tp];
-						if(cut < 0)
+						const int enc = s.px_cut[tp];
+						if(enc > -2)
 							continue;
-						int off = s.px_wbase[tp];
+						const int cut = -2 - enc, wc = s.px_wcnt[tp];
 						for(int c0 = s.px_lo[tp]; c0 <= cut; c0 += 32) {
 							const int bk = c0 + lane;
 							const bool in = bk <= cut;
-							const int v = in ? int(s.hist[histIdx(tp, bk, nb_log)]) : 0;
-							const int incl = warpInclusiveScan(v);
-							const int beg = off + incl - v;
+							const int off = in ? int(s.hist[histIdx(tp, bk, nb_log)]) : 0;
+							const int nxt = in ? (bk < cut ? int(s.hist[histIdx(tp, bk + 1, nb_log)]) : wc) : 0;
+							__syncwarp();
 							if(in)
-								s.hist[histIdx(tp, bk, nb_log)] = uint32_t(beg);
-							off += __shfl_sync(0xffffffffu, incl, 31);
-							big |= addSegments(in, beg, v);
+								s.hist[histIdx(tp, bk, nb_log)] = uint32_t(nxt - off);
+							__syncwarp();
 						}
+						if(lane == 0)
+							s.px_cut[tp] = -1, s.px_wcnt[tp] = 0;
 					}
-				} else {
-					big = addSegments(t < npix && wcount > 0, wbase, wcount);
 				}
 				const bool any_big = __syncthreads_or(big);
 				if(!__syncthreads_or(wcount > 0)) {
@@ -1017,7 +1064,7 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 												 int bk = int((key - slab_lo) >> shift);
 												 if(bk < s.px_lo[tp] || bk > s.px_cut[tp])
 													 return;
-												 pos = int(atomicAdd(&s.hist[histIdx(tp, bk, nb_log)], 1u));
+												 pos = s.px_wbase[tp] + int(atomicAdd(&s.hist[histIdx(tp, bk, nb_log)], 1u));
 											 } else {
 												 pos = atomicAdd(&s.px_wend[tp], 1);
 											 }
@@ -1032,7 +1079,7 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 				// every window segment must be exactly full (histogram and generation evaluate the
 				// same keys); anything else is an internal error
 				if(t < npix && s.px_cut[t] >= 0) {
-					int filled = windowed ? int(s.hist[histIdx(t, s.px_cut[t], nb_log)]) : s.px_wend[t];
+					int filled = windowed ? s.px_wbase[t] + int(s.hist[histIdx(t, s.px_cut[t], nb_log)]) : s.px_wend[t];
 					int want = s.px_wbase[t] + s.px_wcnt[t];
 					if(filled != want)
 						raiseError(p.info, LUCID_ERR_BIN_COUNT, uint32_t(bin), uint32_t(p0 + t),
@@ -1047,22 +1094,37 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 				if(!any_big) {
 					uint32_t* K0 = s.kv[0][0];
 					uint32_t* V0 = s.kv[0][1];
-					const int ns = s.n_small, nl = s.n_large;
+					// one index space over the four size classes, in class order, so that the
+					// lanes of a warp mostly run the same network
+					constexpr int kList = kGroupCap / 2;
+					const unsigned long long nc = s.n_cls;
+					const int e0 = int(nc & 0xffffu), e1 = e0 + int((nc >> 16) & 0xffffu);
+					const int e2 = e1 + int((nc >> 32) & 0xffffu), ns = e2 + int(nc >> 48), nl = s.n_large;
+					// entries of deferred pixels (not in this window) are skipped
 					for(int i = tid; i < ns; i += RT) {
-						const uint32_t e = s.sub_small[i];
-						const int beg = int(e >> 16), cnt = int(e & 0xffffu);
-						if(cnt <= 2)
+						const uint32_t e = i < e0 ? s.sub_small[i]
+										 : i < e1 ? s.radix[i - e0]
+										 : i < e2 ? s.sub_small[kList - 1 - (i - e1)]
+												  : s.radix[kList - 1 - (i - e2)];
+						const int tp = segPixel(e);
+						if(s.px_cut[tp] < 0)
+							continue;
+						const int beg = s.px_wbase[tp] + int(e & 0x1fffu), cnt = segCount(e);
+						if(i < e0)
 							threadSortSegment<2>(K0, V0, beg, cnt);
-						else if(cnt <= 4)
+						else if(i < e1)
 							threadSortSegment<4>(K0, V0, beg, cnt);
-						else if(cnt <= 8)
+						else if(i < e2)
 							threadSortSegment<8>(K0, V0, beg, cnt);
 						else
 							threadSortSegment<16>(K0, V0, beg, cnt);
 					}
 					for(int i = warp; i < nl; i += NW) {
 						const uint32_t e = s.sub_large[i];
-						const int beg = int(e >> 16), cnt = int(e & 0xffffu);
+						const int tp = segPixel(e);
+						if(s.px_cut[tp] < 0)
+							continue;
+						const int beg = s.px_wbase[tp] + int(e & 0x1fffu), cnt = segCount(e);
 						if(cnt <= 32)
 							warpSortSegment<1>(K0, V0, beg, cnt);
 						else if(cnt <= 64)
@@ -1073,6 +1135,9 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 							warpSortSegment<8>(K0, V0, beg, cnt);
 					}
 				}
+				__syncthreads();
+				if(tid == 0) // the lists are consumed: the next window's start empty
+					s.n_cls = 0ull, s.n_large = 0;
 				__syncthreads();
 				RASTER_TIMER(4);
 				const bool use_radix = any_big && n > 1;
@@ -1312,12 +1377,14 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 					s.px_done[t] += s.px_wcnt[t];
 					int next = s.px_cut[t] + 1;
 					s.px_lo[t] = next;
-					if(!windowed)
+					if(!windowed || s.px_done[t] >= s.pix_count[p0 + t]) // every fragment is processed
 						s.px_state[t] = 1;
 					else if(next >= nbuckets) // the slab is used up: wait for the next one, or done
-						s.px_state[t] = (s.px_done[t] < s.pix_count[p0 + t] && slab_hi < s.kmax) ? 2 : 1;
+						s.px_state[t] = slab_hi < s.kmax ? 2 : 1;
 				}
-				__syncthreads();
+				// every pixel finished: no further selection round
+				if(!__syncthreads_or(t < npix && s.px_state[t] != 1))
+					break;
 			}
 
 			// C7. output
