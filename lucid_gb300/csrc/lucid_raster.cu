@@ -1051,29 +1051,49 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 				}
 				const int n = total;
 
-				// C3. window fragments into their sub-segments
-				{
+				// C3. window fragments into their sub-segments. A lane always visits the same pixel,
+				// so its window (as a key range), cursor base and end are read once.
+				if(windowed) {
+					int c_tp = -1, c_base = 0, c_end = 0;
+					uint32_t c_klo = 1u, c_khi = 0u;
 					forEachGroupFragment(p, s, scratch, band_cap, bin_x, bin_y, p0, p1,
 										 [&](int tp, uint32_t key, uint32_t tri) {
-											 if(s.px_cut[tp] < 0)
-												 return;
-											 int pos;
-											 if(windowed) {
-												 if(key < slab_lo || key > slab_hi)
-													 return;
-												 int bk = int((key - slab_lo) >> shift);
-												 if(bk < s.px_lo[tp] || bk > s.px_cut[tp])
-													 return;
-												 pos = s.px_wbase[tp] + int(atomicAdd(&s.hist[histIdx(tp, bk, nb_log)], 1u));
-											 } else {
-												 pos = atomicAdd(&s.px_wend[tp], 1);
+											 if(tp != c_tp) {
+												 c_tp = tp;
+												 const int cut = s.px_cut[tp];
+												 c_klo = 1u, c_khi = 0u;
+												 if(cut >= 0) {
+													 const unsigned long long a = (unsigned long long)slab_lo +
+																				  ((unsigned long long)s.px_lo[tp] << shift);
+													 const unsigned long long z = (unsigned long long)slab_lo +
+																				  ((unsigned long long)(cut + 1) << shift) - 1ull;
+													 c_klo = uint32_t(a);
+													 c_khi = uint32_t(z < (unsigned long long)slab_hi ? z : (unsigned long long)slab_hi);
+												 }
+												 c_base = s.px_wbase[tp];
+												 c_end = c_base + s.px_wcnt[tp];
 											 }
-											 if(pos < s.px_wbase[tp] + s.px_wcnt[tp]) {
+											 if(key < c_klo || key > c_khi)
+												 return;
+											 const int bk = int((key - slab_lo) >> shift);
+											 const int pos = c_base + int(atomicAdd(&s.hist[histIdx(tp, bk, nb_log)], 1u));
+											 if(pos < c_end) {
 												 s.kv[0][0][pos] = key;
 												 s.kv[0][1][pos] = fragPayload(tp, tri);
 											 }
 										 },
-										 windowed ? ekeys : nullptr, slab_lo, shift);
+										 ekeys, slab_lo, shift);
+				} else {
+					forEachGroupFragment(p, s, scratch, band_cap, bin_x, bin_y, p0, p1,
+										 [&](int tp, uint32_t key, uint32_t tri) {
+											 if(s.px_cut[tp] < 0)
+												 return;
+											 const int pos = atomicAdd(&s.px_wend[tp], 1);
+											 if(pos < s.px_wbase[tp] + s.px_wcnt[tp]) {
+												 s.kv[0][0][pos] = key;
+												 s.kv[0][1][pos] = fragPayload(tp, tri);
+											 }
+										 });
 				}
 				__syncthreads();
 				// every window segment must be exactly full (histogram and generation evaluate the
