@@ -389,16 +389,26 @@ __device__ __forceinline__ void forEachGroupFragment(const FrameParams& p, const
 				span = uint32_t(lo) | uint32_t(hi) << 5;
 			}
 		}
-		for(uint32_t todo = __ballot_sync(0xffffffffu, rel); todo != 0u; todo &= todo - 1u) {
-			const int k = __ffs(todo) - 1;
-			const uint32_t sp = __shfl_sync(0xffffffffu, span, k);
-			const float kdx = __shfl_sync(0xffffffffu, dx, k), kty = __shfl_sync(0xffffffffu, ty, k);
-			const uint32_t ktri = __shfl_sync(0xffffffffu, tri, k);
-			const int lo = int(sp & 31u), hi = int(sp >> 5);
-			if(in_group && lane >= lo && lane <= hi) {
-				const float inv_ray_pos = kdx * fx + kty;
-				fn(t, nearFirstKey(inv_ray_pos), ktri);
-			}
+		// two entries per step (in lane order), so that their shuffles and key evaluations overlap
+		uint32_t todo = __ballot_sync(0xffffffffu, rel);
+		while(todo != 0u) {
+			const int k1 = __ffs(todo) - 1;
+			todo &= todo - 1u;
+			const bool two = todo != 0u;
+			const int k2 = two ? __ffs(todo) - 1 : k1;
+			if(two)
+				todo &= todo - 1u;
+			const uint32_t sp1 = __shfl_sync(0xffffffffu, span, k1), sp2 = __shfl_sync(0xffffffffu, span, k2);
+			const float dx1 = __shfl_sync(0xffffffffu, dx, k1), ty1 = __shfl_sync(0xffffffffu, ty, k1);
+			const float dx2 = __shfl_sync(0xffffffffu, dx, k2), ty2 = __shfl_sync(0xffffffffu, ty, k2);
+			const uint32_t tri1 = __shfl_sync(0xffffffffu, tri, k1), tri2 = __shfl_sync(0xffffffffu, tri, k2);
+			const bool c1 = in_group && lane >= int(sp1 & 31u) && lane <= int(sp1 >> 5);
+			const bool c2 = two && in_group && lane >= int(sp2 & 31u) && lane <= int(sp2 >> 5);
+			const uint32_t key1 = nearFirstKey(dx1 * fx + ty1), key2 = nearFirstKey(dx2 * fx + ty2);
+			if(c1)
+				fn(t, key1, tri1);
+			if(c2)
+				fn(t, key2, tri2);
 		}
 	}
 }
