@@ -67,6 +67,8 @@ struct FrameParams {
 	uint4* quad_normals;  // encoded vertex normals per quad slot (STORAGE_QUAD_NORMAL)
 	uint4* quad_tex;      // 2 per quad slot: tex0, tex1 - tex0, tex2 - tex0, tex3 - tex0
 	uint4* tri_bary;  // 2 per tri
+	uint4* tri_shade; // 3 per tri: the two tri_bary records, then the tri's RGBA8 vertex colours
+	                  // (when the instance has them) and its instance flags | id << 16
 	uint4* tri_scan;  // 2 per tri
 	uint4* tri_depth; // 1 per tri
 	uint32_t* tri_normals;

@@ -85,6 +85,7 @@ struct lucid_renderer {
 	uint4* quad_normals = nullptr;
 	uint4* quad_tex = nullptr;
 	uint4* tri_bary = nullptr;
+	uint4* tri_shade = nullptr;
 	uint4* tri_scan = nullptr;
 	uint4* tri_depth = nullptr;
 	uint32_t* tri_normals = nullptr;
@@ -222,6 +223,7 @@ FrameParams makeParams(lucid_renderer* r, const lucid_frame_inputs* in, float* o
 	p.quad_normals = r->quad_normals;
 	p.quad_tex = r->quad_tex;
 	p.tri_bary = r->tri_bary;
+	p.tri_shade = r->tri_shade;
 	p.tri_scan = r->tri_scan;
 	p.tri_depth = r->tri_depth;
 	p.tri_normals = r->tri_normals;
@@ -458,6 +460,7 @@ extern "C" lucid_status lucid_create(const lucid_options* options, int32_t width
 	   (st = allocate(r, &r->quad_normals, mvq)) != LUCID_OK ||
 	   (st = allocate(r, &r->quad_tex, 2 * mvq)) != LUCID_OK ||
 	   (st = allocate(r, &r->tri_bary, 4 * mvq)) != LUCID_OK ||
+	   (st = allocate(r, &r->tri_shade, 6 * mvq)) != LUCID_OK ||
 	   (st = allocate(r, &r->tri_scan, 4 * mvq)) != LUCID_OK ||
 	   (st = allocate(r, &r->tri_depth, 2 * mvq)) != LUCID_OK ||
 	   (st = allocate(r, &r->tri_normals, 2 * mvq)) != LUCID_OK ||
@@ -1052,6 +1055,7 @@ void batchParams(lucid_renderer* r, BatchPlan* b, const lucid_view* views, std::
 		p.quad_normals = r->quad_normals + qbase;
 		p.quad_tex = r->quad_tex + 2 * qbase;
 		p.tri_bary = r->tri_bary + 4 * qbase;
+		p.tri_shade = r->tri_shade + 6 * qbase;
 		p.tri_scan = r->tri_scan + 4 * qbase;
 		p.tri_depth = r->tri_depth + 2 * qbase;
 		p.tri_normals = r->tri_normals + 2 * qbase;

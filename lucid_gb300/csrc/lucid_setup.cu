@@ -208,7 +208,7 @@ __device__ __forceinline__ QuadClass processInputQuad(const FrameParams& p, cons
 // storeTri (quad_setup.glsl:274-340)
 __device__ __forceinline__ void storeTri(const FrameParams& p, const lucid_config& cfg, F3 ray_dir0,
 						 uint32_t tri_idx, uint32_t inst_flags_id, F3 tri0, F3 tri1, F3 tri2,
-						 uint32_t y_aabb) {
+						 uint32_t y_aabb, uint3 colors) {
 	F3 dirx = xyz4(cfg.frustum.ws_dirx), diry = xyz4(cfg.frustum.ws_diry);
 	F3 dir0 = xyz4(cfg.frustum.ws_dir0);
 	F3 normal = cross3(tri0 - tri2, tri1 - tri0);
@@ -233,10 +233,14 @@ __device__ __forceinline__ void storeTri(const FrameParams& p, const lucid_confi
 	F3 pnormal = normal * (1.0f / plane_dist);
 	F3 deq = f3(dot3(pnormal, dirx), dot3(pnormal, diry), dot3(pnormal, ray_dir0));
 	p.tri_depth[tri_idx] = make_uint4(fbits(deq.x), fbits(deq.y), fbits(deq.z), inst_flags_id);
-	p.tri_bary[size_t(tri_idx) * 2 + 0] =
-		make_uint4(fbits(e0.x), fbits(e0.y), fbits(e0.z), fbits(param0));
-	p.tri_bary[size_t(tri_idx) * 2 + 1] =
-		make_uint4(fbits(e1.x), fbits(e1.y), fbits(e1.z), fbits(param1));
+	const uint4 bary0 = make_uint4(fbits(e0.x), fbits(e0.y), fbits(e0.z), fbits(param0));
+	const uint4 bary1 = make_uint4(fbits(e1.x), fbits(e1.y), fbits(e1.z), fbits(param1));
+	p.tri_bary[size_t(tri_idx) * 2 + 0] = bary0;
+	p.tri_bary[size_t(tri_idx) * 2 + 1] = bary1;
+	// the shading record: what a fragment of the tri reads, in 48 contiguous bytes
+	p.tri_shade[size_t(tri_idx) * 3 + 0] = bary0;
+	p.tri_shade[size_t(tri_idx) * 3 + 1] = bary1;
+	p.tri_shade[size_t(tri_idx) * 3 + 2] = make_uint4(colors.x, colors.y, colors.z, inst_flags_id);
 
 	F3 nrm0 = cross3(tri2, tri1 - tri2);
 	F3 nrm1 = cross3(tri0, tri2 - tri0);
@@ -419,10 +423,11 @@ template <class Src> __global__ void __launch_bounds__(kSetupThreads) setupStore
 	p.quad_source[slot] = uint32_t(q);
 	p.quad_verts[slot] = make_uint4(v[0], v[1], v[2], v[3]);
 	uint32_t flags = uint32_t(p.instances[inst].flags);
+	uint4 qc = make_uint4(0u, 0u, 0u, 0u);
 	if((flags & LUCID_INST_HAS_VERTEX_COLORS) && p.color_format == LUCID_COLOR_RGBA8) {
 		const uint32_t* cols = reinterpret_cast<const uint32_t*>(p.colors);
-		p.quad_colors[slot] =
-			make_uint4(__ldg(cols + v[0]), __ldg(cols + v[1]), __ldg(cols + v[2]), __ldg(cols + v[3]));
+		qc = make_uint4(__ldg(cols + v[0]), __ldg(cols + v[1]), __ldg(cols + v[2]), __ldg(cols + v[3]));
+		p.quad_colors[slot] = qc;
 	}
 	// storeQuad (quad_setup.glsl:256-272): vertex normals, texture coordinates relative to the
 	// first vertex
@@ -450,7 +455,7 @@ template <class Src> __global__ void __launch_bounds__(kSetupThreads) setupStore
 		F3 t1 = loadVertex(p.positions, v[1 + second]) - origin;
 		F3 t2 = loadVertex(p.positions, v[2 + second]) - origin;
 		storeTri(p, cfg, ray_dir0, uint32_t(slot) * 2 + second, inst_flags_id, t0, t1, t2,
-				 second ? rec.z : rec.y);
+				 second ? rec.z : rec.y, make_uint3(qc.x, second ? qc.z : qc.y, second ? qc.w : qc.z));
 	}
 }
 

@@ -118,9 +118,10 @@ struct ShadeCore {
 
 __device__ __forceinline__ ShadeCore shadeCore(const FrameParams& p, uint32_t tri, float inv_ray_pos, int px, int py) {
 	ShadeCore s;
-	const uint4 b0r = __ldg(p.tri_bary + size_t(tri) * 2);
-	const uint4 b1r = __ldg(p.tri_bary + size_t(tri) * 2 + 1);
-	const uint32_t fid = __ldg(&p.tri_depth[tri].w);
+	// the tri's shading record: barycentric planes, RGBA8 vertex colours, instance flags and id
+	const uint4* rec = p.tri_shade + size_t(tri) * 3;
+	const uint4 b0r = __ldg(rec), b1r = __ldg(rec + 1), crec = __ldg(rec + 2);
+	const uint32_t fid = crec.w;
 	const float fx = float(px), fy = float(py);
 	const float ray_pos = 1.0f / inv_ray_pos;
 	const float e0 = bitsf(b0r.x) * fx + (bitsf(b0r.y) * fy + bitsf(b0r.z));
@@ -172,10 +173,9 @@ __device__ __forceinline__ ShadeCore shadeCore(const FrameParams& p, uint32_t tr
 		s.vid[0] = qv.x, s.vid[1] = second ? qv.z : qv.y, s.vid[2] = second ? qv.w : qv.z;
 		float4 c0, c1, c2;
 		if(p.color_format == LUCID_COLOR_RGBA8) {
-			const uint4 qc = __ldg(p.quad_colors + quad);
-			c0 = decodeRGBA8(qc.x);
-			c1 = decodeRGBA8(second ? qc.z : qc.y);
-			c2 = decodeRGBA8(second ? qc.w : qc.z);
+			c0 = decodeRGBA8(crec.x);
+			c1 = decodeRGBA8(crec.y);
+			c2 = decodeRGBA8(crec.z);
 		} else if(p.color_format == LUCID_COLOR_RGBA16F) {
 			const uint2* hc = reinterpret_cast<const uint2*>(p.colors);
 			const uint2 h0 = __ldg(hc + s.vid[0]), h1 = __ldg(hc + s.vid[1]), h2 = __ldg(hc + s.vid[2]);
