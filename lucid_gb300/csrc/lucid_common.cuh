@@ -78,6 +78,7 @@ struct FrameParams {
 	uint32_t* raster_work; // bin_count bin ids: HIGH, LOW, EMPTY
 	uint2* band_scratch;  // per raster CTA: 8 * band_capacity entries
 	uint2* band_keys;     // per raster CTA and band entry: depth-key range over the current group
+	float4* band_planes;  // per raster CTA and band entry: the tri's depth plane (dx, dy, dz)
 	int* dump_counts;     // verification mode (may be null)
 	int* dump_prims;
 	int dump_max;

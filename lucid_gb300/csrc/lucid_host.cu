@@ -95,6 +95,7 @@ struct lucid_renderer {
 	uint32_t* raster_work = nullptr;
 	uint2* band_scratch = nullptr;
 	uint2* band_keys = nullptr;
+	float4* band_planes = nullptr;
 	uint8_t* ref_plan = nullptr; // reference-order mode: path of every bin
 
 	FrameParams last{}; // parameters of the last quad setup (used by the later passes)
@@ -233,6 +234,7 @@ FrameParams makeParams(lucid_renderer* r, const lucid_frame_inputs* in, float* o
 	p.raster_work = r->raster_work;
 	p.band_scratch = r->band_scratch;
 	p.band_keys = r->band_keys;
+	p.band_planes = r->band_planes;
 	return p;
 }
 
@@ -470,6 +472,7 @@ extern "C" lucid_status lucid_create(const lucid_options* options, int32_t width
 	   (st = allocate(r, &r->raster_work, size_t(r->bin_count))) != LUCID_OK ||
 	   (st = allocate(r, &r->band_scratch, size_t(r->raster_ctas) * 8 * o.band_capacity)) != LUCID_OK ||
 	   (st = allocate(r, &r->band_keys, size_t(r->raster_ctas) * 8 * o.band_capacity)) != LUCID_OK ||
+	   (st = allocate(r, &r->band_planes, size_t(r->raster_ctas) * 8 * o.band_capacity)) != LUCID_OK ||
 	   (st = allocate(r, &r->ref_plan, size_t(r->bin_count))) != LUCID_OK)
 		return bail(st);
 	// zero the records once so that unused slots read as zero in parity dumps
@@ -1065,6 +1068,7 @@ void batchParams(lucid_renderer* r, BatchPlan* b, const lucid_view* views, std::
 		p.raster_work = b->raster_work + rbase;
 		p.band_scratch = r->band_scratch;
 		p.band_keys = r->band_keys;
+		p.band_planes = r->band_planes;
 		p.ref_alloc = b->counters;
 		qbase += size_t(cap);
 		ibase += size_t(in.num_instances) + 1;

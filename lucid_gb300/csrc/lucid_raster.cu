@@ -325,7 +325,7 @@ __device__ void writePixel(const FrameParams& p, int px, int py, float4 c) {
 // With `ekeys` and flo <= fhi, entries are culled against the fixed key range [flo, fhi] instead.
 template <typename Fn>
 __device__ __forceinline__ void forEachGroupFragment(const FrameParams& p, const RasterSmem& s,
-													  const uint2* scratch, int band_cap, int bin_x,
+													  const uint2* scratch, const float4* planes, int band_cap, int bin_x,
 													  int bin_y, int p0, int p1, Fn fn,
 													  const uint2* ekeys = nullptr, uint32_t kmin = 0u,
 													  int shift = 0, uint32_t flo = 1u, uint32_t fhi = 0u) {
@@ -379,13 +379,13 @@ __device__ __forceinline__ void forEachGroupFragment(const FrameParams& p, const
 		float dx = 0.0f, ty = 0.0f;
 		if(rel) {
 			const uint2 e = scratch[size_t(b) * band_cap + j];
+			const float4 d = planes[size_t(b) * band_cap + j];
 			const int lo = (e.x >> rshift) & 31, hi = (e.y >> rshift) & 31;
 			rel = max(lo, glo) <= min(hi, ghi);
 			if(rel) {
 				tri = entryTri(e);
-				const uint4 d = __ldg(p.tri_depth + tri);
-				dx = bitsf(d.x);
-				ty = bitsf(d.y) * fy + bitsf(d.z);
+				dx = d.x;
+				ty = d.y * fy + d.z;
 				span = uint32_t(lo) | uint32_t(hi) << 5;
 			}
 		}
@@ -492,6 +492,7 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 	const int band_cap = p_first.band_capacity;
 	uint2* scratch = p_first.band_scratch + size_t(blockIdx.x) * 8 * band_cap;
 	uint2* ekeys = p_first.band_keys + size_t(blockIdx.x) * 8 * band_cap;
+	float4* planes = p_first.band_planes + size_t(blockIdx.x) * 8 * band_cap;
 	const uint32_t opt_flags = p_first.flags;
 	const bool additive = (opt_flags & LUCID_OPT_ADDITIVE_BLENDING) != 0;
 	const bool alpha_threshold = (opt_flags & LUCID_OPT_ALPHA_THRESHOLD) != 0;
@@ -561,6 +562,8 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 			}
 			uint4 r0 = __ldg(p.tri_scan + size_t(tri) * 2);
 			uint4 r1 = __ldg(p.tri_scan + size_t(tri) * 2 + 1);
+			const uint4 dq = __ldg(p.tri_depth + tri);
+			const float4 plane = make_float4(bitsf(dq.x), bitsf(dq.y), bitsf(dq.z), 0.0f);
 			int ymin = int(r0.w & 0xffffu) - bin_y, ymax = int(r0.w >> 16) - bin_y;
 			int min_by = min(max(ymin, 0), 31) >> 3, max_by = min(max(ymax, 0), 31) >> 3;
 			float sx = float(bin_x), sy = float(bin_y + min_by * 8);
@@ -605,9 +608,11 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 				hbt += __popc(colmask);
 				if(nonempty) {
 					int slot = atomicAdd(&s.band_count[band], 1);
-					if(slot < band_cap)
+					if(slot < band_cap) {
 						scratch[size_t(band) * band_cap + slot] =
 							make_uint2(minb | ((tri & 0xfffu) << 20), maxb | ((tri >> 12) << 20));
+						planes[size_t(band) * band_cap + slot] = plane;
+					}
 				}
 			}
 		}
@@ -772,8 +777,8 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 					const int ne = s.band_count[b];
 					for(int j = tid; j < ne; j += RT) {
 						uint2 e = scratch[size_t(b) * band_cap + j];
-						uint4 d = __ldg(p.tri_depth + entryTri(e));
-						float dx = bitsf(d.x), dy = bitsf(d.y), dz = bitsf(d.z);
+						const float4 d = planes[size_t(b) * band_cap + j];
+						float dx = d.x, dy = d.y, dz = d.z;
 						uint32_t emn = 0xffffffffu, emx = 0u;
 						int wsum = 0;
 #pragma unroll
@@ -876,14 +881,14 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 				// entries are culled against the slab only when it is narrower than the group's keys
 				const bool cull = lo_k > s.kmin || hi_k < s.kmax;
 				if(cull)
-					forEachGroupFragment(p, s, scratch, band_cap, bin_x, bin_y, p0, p1,
+					forEachGroupFragment(p, s, scratch, planes, band_cap, bin_x, bin_y, p0, p1,
 										 [&](int tp, uint32_t key, uint32_t) {
 											 if(key >= lo_k && key <= hi_k)
 												 atomicAdd(&s.hist[histIdx(tp, int((key - lo_k) >> sh), nb_log)], 1u);
 										 },
 										 ekeys, 0u, 0, lo_k, hi_k);
 				else // the whole key range: no test per fragment
-					forEachGroupFragment(p, s, scratch, band_cap, bin_x, bin_y, p0, p1,
+					forEachGroupFragment(p, s, scratch, planes, band_cap, bin_x, bin_y, p0, p1,
 										 [&](int tp, uint32_t key, uint32_t) {
 											 atomicAdd(&s.hist[histIdx(tp, int((key - lo_k) >> sh), nb_log)], 1u);
 										 });
@@ -1066,7 +1071,7 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 				if(windowed) {
 					int c_tp = -1, c_base = 0, c_end = 0;
 					uint32_t c_klo = 1u, c_khi = 0u;
-					forEachGroupFragment(p, s, scratch, band_cap, bin_x, bin_y, p0, p1,
+					forEachGroupFragment(p, s, scratch, planes, band_cap, bin_x, bin_y, p0, p1,
 										 [&](int tp, uint32_t key, uint32_t tri) {
 											 if(tp != c_tp) {
 												 c_tp = tp;
@@ -1094,7 +1099,7 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 										 },
 										 ekeys, slab_lo, shift);
 				} else {
-					forEachGroupFragment(p, s, scratch, band_cap, bin_x, bin_y, p0, p1,
+					forEachGroupFragment(p, s, scratch, planes, band_cap, bin_x, bin_y, p0, p1,
 										 [&](int tp, uint32_t key, uint32_t tri) {
 											 if(s.px_cut[tp] < 0)
 												 return;
