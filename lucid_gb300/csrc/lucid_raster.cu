@@ -12,21 +12,23 @@
 //     viewport. A shared +1/-1 difference array per row counts fragments per pixel.
 //  B. Pixel groups. The bin's pixels (row-major) are cut into groups of at most 256 pixels
 //     whose fragments, each pixel counted up to kWindow, fit kGroupBudget.
-//  C. Depth windows. A group whose pixels all have <= kWindow fragments is one window. In a
-//     heavier group every pixel gets a coarse histogram of its depth keys (buckets of the
-//     group's key range); a pixel's window is the run of buckets, from the first one it has
-//     not processed, that holds >= kWindow fragments. Buckets split the key space in order,
-//     so windows visit each pixel's fragments strictly front to back.
-//  D. Per window: fragments (32-bit nearest-first depth key, 32-bit payload = pixel | band |
-//     entry) are generated by one warp per pixel row (lane = pixel, band entries broadcast by
-//     shuffle) and written to their pixel's segment, in a heavy group to the sub-segment of
-//     their depth bucket. Sub-segments are sorted by key (one thread per small sub-segment with
-//     a register network, one warp per larger one with a bitonic network; a block-wide radix
-//     sort when one exceeds 256). Runs of equal depth are put in primitive-id order. Shading
-//     runs in parallel batches; one thread per pixel blends front to back in FP32
-//     (out += rgb*a*T; T *= 1-a, shading.glsl:279-280) and stops once T == 0: no later
-//     fragment can change the pixel (it adds rgb*a*0). Background is added last
-//     (shading.glsl:312).
+//  C. Depth windows. A group whose pixels all have <= kHeavyPixel fragments is one window. In
+//     a heavier group every pixel gets a coarse histogram of its depth keys (buckets of one
+//     depth slab of the group's key range); a pixel's window is the run of buckets, from the
+//     first one it has not processed, that holds >= kWindow fragments. Buckets split the key
+//     space in order, so windows visit each pixel's fragments strictly front to back. A slab
+//     covers about slab_target fragments per unfinished pixel (from an estimate gathered with
+//     the group's key range); the next slab is counted only if a pixel needs it.
+//  D. Per window: fragments (32-bit nearest-first depth key, 32-bit payload = pixel | tri) are
+//     generated by one warp per pixel row (lane = pixel, band entries broadcast by shuffle) and
+//     written to their pixel's segment, in a heavy group to the sub-segment of their depth
+//     bucket. Sub-segments are sorted by key (one thread per small sub-segment with a register
+//     network, grouped by size; one warp per larger one with a bitonic network; a block-wide
+//     radix sort when one exceeds 256). Runs of equal depth are put in primitive-id order.
+//     Shading runs in parallel batches from each tri's 48-byte shading record; one thread per
+//     pixel blends front to back in FP32 (out += rgb*a*T; T *= 1-a, shading.glsl:279-280) and
+//     stops once T == 0: no later fragment can change the pixel (it adds rgb*a*0). Background
+//     is added last (shading.glsl:312).
 
 #include "lucid_common.cuh"
 #include "lucid_kernels.h"
@@ -40,6 +42,10 @@ constexpr int kGroupCap = 8192;     // fragments per window (shared-memory sort 
 constexpr int kGroupPixels = 256;   // pixels per group (8-bit pixel index in the payload)
 constexpr int kStage = 4096;        // shaded fragments per shading round (64 KB of float4)
 constexpr int kWindow = 176;        // target fragments per pixel per depth window
+// a group with a pixel of more fragments is processed in depth windows: the histogram buckets
+// split its pixels' lists into small sub-segments (cheap thread sorts instead of warp sorts of
+// whole lists)
+constexpr int kHeavyPixel = 32;
 constexpr int kGroupBudget = 6144;  // sum over a group's pixels of min(count, kWindow)
 constexpr int kHistWords = 8192;    // per-group depth histogram (pixels x buckets)
 constexpr int kCoarseShift = 20;    // fragment estimate bins: depth keys >> 20 (4096 bins)
@@ -729,7 +735,7 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 			}
 			if(t < npix) {
 				int c = s.pix_count[p0 + t];
-				heavy = c > kWindow;
+				heavy = c > kHeavyPixel;
 				s.px_T[t] = 1.0f;
 				s.px_c[t][0] = s.px_c[t][1] = s.px_c[t][2] = 0.0f;
 				s.px_lo[t] = 0;
