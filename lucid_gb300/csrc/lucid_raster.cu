@@ -41,6 +41,8 @@ constexpr int NW = RT / 32;
 constexpr int kGroupCap = 8192;     // fragments per window (shared-memory sort capacity)
 constexpr int kGroupPixels = 256;   // pixels per group (8-bit pixel index in the payload)
 constexpr int kStage = 4096;        // shaded fragments per shading round (64 KB of float4)
+constexpr int kShadeFirst = 128;    // fragments per pixel in a window's first shading round
+constexpr int kShadeNext = 32;      // ... and in its later rounds
 constexpr int kWindow = 176;        // target fragments per pixel per depth window
 // a group with a pixel of more fragments is processed in depth windows: the histogram buckets
 // split its pixels' lists into small sub-segments (cheap thread sorts instead of warp sorts of
@@ -908,9 +910,6 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 			if(windowed)
 				buildSlab(0);
 			RASTER_TIMER(2);
-			// fragments shaded per pixel per round: fewer pixels, deeper batches
-			// (odd, so that the pixels' staging rows start in different shared-memory banks)
-			const int batch = (min(256, kStage / max(npix, 1)) - 1) | 1;
 
 			// C2. windows
 			while(true) {
@@ -1243,7 +1242,12 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 					}
 					__syncthreads();
 				}
-				while(MODE != kRasterStore) {
+				for(int round = 0; MODE != kRasterStore; round++) {
+					// fragments shaded per pixel in this round: the first round's batch covers
+					// what most pixels need to reach T == 0, later ones are shorter so that
+					// little is shaded behind that point; odd, so that the pixels' staging rows
+					// start in different shared-memory banks
+					const int batch = (min(round == 0 ? kShadeFirst : kShadeNext, kStage / max(npix, 1)) - 1) | 1;
 					if constexpr(MODE != kRasterBackward) {
 						// slot / batch by multiply and shift (exact for odd batch in [15, 255] and
 						// slot < 4096)
