@@ -920,32 +920,37 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 				// holding >= kWindow fragments and turns the bucket counts into relative cursors.
 				// List slots come from warp-aggregated counters; an entry is
 				// (relative start, count, pixel), see segEntry.
-				auto addSegments = [&](bool in, int beg, int c, int tp) {
+				// one sub-segment per lane of each of two pixels A and B: class masks by ballot, one
+				// packed atomic for the slots of both (A's entries first)
+				auto addSegments2 = [&](bool inA, int begA, int cA, int tpA, bool inB, int begB, int cB, int tpB) {
 					constexpr int kList = kGroupCap / 2;
-					const uint32_t entry = segEntry(beg, c, tp);
-					const int cls = c <= 2 ? 0 : c <= 4 ? 1 : c <= 8 ? 2 : 3;
-					const bool sm = in && c >= 2 && c <= 16, lg = in && c > 16 && c <= 256;
-					const uint32_t msm = __ballot_sync(0xffffffffu, sm), mlg = __ballot_sync(0xffffffffu, lg);
-					if(msm | mlg) {
-						const uint32_t b0 = __ballot_sync(0xffffffffu, cls & 1), b1 = __ballot_sync(0xffffffffu, cls & 2);
-						const uint32_t mc0 = msm & ~b0 & ~b1, mc1 = msm & b0 & ~b1, mc2 = msm & ~b0 & b1, mc3 = msm & b0 & b1;
+					const uint32_t lt = laneMaskLt();
+					const bool smA = inA && cA >= 2 && cA <= 16, lgA = inA && cA > 16 && cA <= 256;
+					const bool smB = inB && cB >= 2 && cB <= 16, lgB = inB && cB > 16 && cB <= 256;
+					const uint32_t msmA = __ballot_sync(0xffffffffu, smA), mlgA = __ballot_sync(0xffffffffu, lgA);
+					const uint32_t msmB = __ballot_sync(0xffffffffu, smB), mlgB = __ballot_sync(0xffffffffu, lgB);
+					if(msmA | mlgA | msmB | mlgB) {
+						const int clsA = cA <= 2 ? 0 : cA <= 4 ? 1 : cA <= 8 ? 2 : 3;
+						const int clsB = cB <= 2 ? 0 : cB <= 4 ? 1 : cB <= 8 ? 2 : 3;
+						const uint32_t a0 = __ballot_sync(0xffffffffu, clsA & 1), a1 = __ballot_sync(0xffffffffu, clsA & 2);
+						const uint32_t b0 = __ballot_sync(0xffffffffu, clsB & 1), b1 = __ballot_sync(0xffffffffu, clsB & 2);
+						const uint32_t mA[4] = {msmA & ~a0 & ~a1, msmA & a0 & ~a1, msmA & ~a0 & a1, msmA & a0 & a1};
+						const uint32_t mB[4] = {msmB & ~b0 & ~b1, msmB & b0 & ~b1, msmB & ~b0 & b1, msmB & b0 & b1};
+						unsigned long long add = 0ull;
+#pragma unroll
+						for(int k = 0; k < 4; k++)
+							add |= (unsigned long long)(__popc(mA[k]) + __popc(mB[k])) << (16 * k);
 						unsigned long long base = 0ull;
 						int lbase = 0;
 						if(lane == 0) {
-							if(msm)
-								base = atomicAdd(&s.n_cls, (unsigned long long)__popc(mc0) |
-															   (unsigned long long)__popc(mc1) << 16 |
-															   (unsigned long long)__popc(mc2) << 32 |
-															   (unsigned long long)__popc(mc3) << 48);
-							if(mlg)
-								lbase = atomicAdd(&s.n_large, __popc(mlg));
+							if(add)
+								base = atomicAdd(&s.n_cls, add);
+							if(mlgA | mlgB)
+								lbase = atomicAdd(&s.n_large, __popc(mlgA) + __popc(mlgB));
 						}
 						base = __shfl_sync(0xffffffffu, base, 0);
 						lbase = __shfl_sync(0xffffffffu, lbase, 0);
-						const uint32_t lt = laneMaskLt();
-						if(sm) {
-							const uint32_t mine = cls == 0 ? mc0 : cls == 1 ? mc1 : cls == 2 ? mc2 : mc3;
-							const int pos = int((base >> (16 * cls)) & 0xffffu) + __popc(mine & lt);
+						auto put = [&](int cls, int pos, uint32_t entry) {
 							if(cls == 0)
 								s.sub_small[pos] = entry;
 							else if(cls == 1)
@@ -954,40 +959,80 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 								s.sub_small[kList - 1 - pos] = entry;
 							else
 								s.radix[kList - 1 - pos] = entry;
+						};
+#pragma unroll
+						for(int k = 0; k < 4; k++) {
+							const int bk = int((base >> (16 * k)) & 0xffffu);
+							if(smA && clsA == k)
+								put(k, bk + __popc(mA[k] & lt), segEntry(begA, cA, tpA));
+							if(smB && clsB == k)
+								put(k, bk + __popc(mA[k]) + __popc(mB[k] & lt), segEntry(begB, cB, tpB));
 						}
-						if(lg)
-							s.sub_large[lbase + __popc(mlg & lt)] = entry;
+						if(lgA)
+							s.sub_large[lbase + __popc(mlgA & lt)] = segEntry(begA, cA, tpA);
+						if(lgB)
+							s.sub_large[lbase + __popc(mlgA) + __popc(mlgB & lt)] = segEntry(begB, cB, tpB);
 					}
-					return in && c > 256;
+					return (inA && cA > 256) || (inB && cB > 256);
+				};
+				auto addSegments = [&](bool in, int beg, int c, int tp) {
+					return addSegments2(in, beg, c, tp, false, 0, 0, 0);
 				};
 				bool big = false;
 				if(windowed) {
-					for(int tp = warp; tp < npix; tp += NW) {
-						if(s.px_state[tp] != 0)
-							continue;
-						int acc = 0, cut = nbuckets - 1;
-						for(int c0 = s.px_lo[tp]; c0 < nbuckets; c0 += 32) {
-							const int bk = c0 + lane;
-							const int v = bk < nbuckets ? int(s.hist[histIdx(tp, bk, nb_log)]) : 0;
-							const int incl = warpInclusiveScan(v);
-							const uint32_t hit = __ballot_sync(0xffffffffu, bk < nbuckets && acc + incl >= kWindow);
-							const int last = hit ? __ffs(hit) - 1 : 31;
-							const bool in = bk < nbuckets && lane <= last;
-							const int rel = acc + incl - v;
-							if(in)
-								s.hist[histIdx(tp, bk, nb_log)] = uint32_t(rel);
-							big |= addSegments(in, rel, v, tp);
-							acc += __shfl_sync(0xffffffffu, incl, last);
-							if(hit) {
-								cut = c0 + last;
-								break;
+					// two pixels per warp at a time (A = tp, B = tp + NW), so that their dependent
+					// steps overlap; each walks its buckets 32 at a time
+					for(int tp = warp; tp < npix; tp += 2 * NW) {
+						const int tpA = tp, tpB = tp + NW;
+						bool doneA = s.px_state[tpA] != 0, doneB = tpB >= npix || s.px_state[tpB] != 0;
+						int accA = 0, cutA = nbuckets - 1, c0A = doneA ? 0 : s.px_lo[tpA];
+						int accB = 0, cutB = nbuckets - 1, c0B = doneB ? 0 : s.px_lo[tpB];
+						const bool actA = !doneA, actB = !doneB;
+						while(!(doneA && doneB)) {
+							const int bkA = c0A + lane, bkB = c0B + lane;
+							const bool okA = !doneA && bkA < nbuckets, okB = !doneB && bkB < nbuckets;
+							const int vA = okA ? int(s.hist[histIdx(tpA, bkA, nb_log)]) : 0;
+							const int vB = okB ? int(s.hist[histIdx(tpB, bkB, nb_log)]) : 0;
+							const int inclA = warpInclusiveScan(vA), inclB = warpInclusiveScan(vB);
+							const uint32_t hitA = __ballot_sync(0xffffffffu, okA && accA + inclA >= kWindow);
+							const uint32_t hitB = __ballot_sync(0xffffffffu, okB && accB + inclB >= kWindow);
+							const int lastA = hitA ? __ffs(hitA) - 1 : 31, lastB = hitB ? __ffs(hitB) - 1 : 31;
+							const bool inA = okA && lane <= lastA, inB = okB && lane <= lastB;
+							const int relA = accA + inclA - vA, relB = accB + inclB - vB;
+							if(inA)
+								s.hist[histIdx(tpA, bkA, nb_log)] = uint32_t(relA);
+							if(inB)
+								s.hist[histIdx(tpB, bkB, nb_log)] = uint32_t(relB);
+							big |= addSegments2(inA, relA, vA, tpA, inB, relB, vB, tpB);
+							const int stA = __shfl_sync(0xffffffffu, inclA, lastA), stB = __shfl_sync(0xffffffffu, inclB, lastB);
+							if(!doneA) {
+								accA += stA;
+								if(hitA)
+									cutA = c0A + lastA, doneA = true;
+								else if((c0A += 32) >= nbuckets)
+									doneA = true;
+							}
+							if(!doneB) {
+								accB += stB;
+								if(hitB)
+									cutB = c0B + lastB, doneB = true;
+								else if((c0B += 32) >= nbuckets)
+									doneB = true;
 							}
 						}
 						if(lane == 0) {
-							s.px_cut[tp] = cut;
-							s.px_wcnt[tp] = acc;
-							if(acc == 0) // nothing left in this slab: wait for the next one, or done
-								s.px_state[tp] = (s.px_done[tp] < s.pix_count[p0 + tp] && s.slab_hi < s.kmax) ? 2 : 1;
+							if(actA) {
+								s.px_cut[tpA] = cutA;
+								s.px_wcnt[tpA] = accA;
+								if(accA == 0) // nothing left in this slab: wait for the next one, or done
+									s.px_state[tpA] = (s.px_done[tpA] < s.pix_count[p0 + tpA] && s.slab_hi < s.kmax) ? 2 : 1;
+							}
+							if(actB) {
+								s.px_cut[tpB] = cutB;
+								s.px_wcnt[tpB] = accB;
+								if(accB == 0)
+									s.px_state[tpB] = (s.px_done[tpB] < s.pix_count[p0 + tpB] && s.slab_hi < s.kmax) ? 2 : 1;
+							}
 						}
 					}
 				} else {
