@@ -11,7 +11,8 @@
 //     layout of raster_high.glsl:85-88) in this CTA's band scratch; spans are clipped to the
 //     viewport. A shared +1/-1 difference array per row counts fragments per pixel.
 //  B. Pixel groups. The bin's pixels (row-major) are cut into groups of at most 256 pixels
-//     whose fragments, each pixel counted up to kWindow, fit kGroupBudget.
+//     whose fragments, each pixel counted up to kWindow, fit kGroupBudget; a group ends at a
+//     row boundary when it holds one.
 //  C. Depth windows. A group whose pixels all have <= kHeavyPixel fragments is one window. In
 //     a heavier group every pixel gets a coarse histogram of its depth keys (buckets of one
 //     depth slab of the group's key range); a pixel's window is the run of buckets, from the
@@ -43,7 +44,7 @@ constexpr int kGroupPixels = 256;   // pixels per group (8-bit pixel index in th
 constexpr int kStage = 4096;        // shaded fragments per shading round (64 KB of float4)
 constexpr int kShadeFirst = 128;    // fragments per pixel in a window's first shading round
 constexpr int kShadeNext = 32;      // ... and in its later rounds
-constexpr int kWindow = 176;        // target fragments per pixel per depth window
+constexpr int kWindow = 160;        // target fragments per pixel per depth window
 // a group with a pixel of more fragments is processed in depth windows: the histogram buckets
 // split its pixels' lists into small sub-segments (cheap thread sorts instead of warp sorts of
 // whole lists)
@@ -713,6 +714,10 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 					else
 						hi = mid - 1;
 				}
+				// end the group at a row boundary when it holds one: a group's passes visit the band
+				// entries of every row it touches, and a row split between two groups is visited twice
+				if((lo & 31) != 0 && (lo & ~31) > p0)
+					lo &= ~31;
 				s.group_end = lo;
 				s.kmin = 0xffffffffu;
 				s.kmax = 0u;
