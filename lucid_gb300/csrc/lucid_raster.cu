@@ -398,26 +398,35 @@ __device__ __forceinline__ void forEachGroupFragment(const FrameParams& p, const
 				span = uint32_t(lo) | uint32_t(hi) << 5;
 			}
 		}
-		// two entries per step (in lane order), so that their shuffles and key evaluations overlap
+		// up to four entries per step (in lane order), so that their shuffles, key evaluations and
+		// the callbacks' shared-memory round trips overlap
 		uint32_t todo = __ballot_sync(0xffffffffu, rel);
 		while(todo != 0u) {
-			const int k1 = __ffs(todo) - 1;
-			todo &= todo - 1u;
-			const bool two = todo != 0u;
-			const int k2 = two ? __ffs(todo) - 1 : k1;
-			if(two)
-				todo &= todo - 1u;
-			const uint32_t sp1 = __shfl_sync(0xffffffffu, span, k1), sp2 = __shfl_sync(0xffffffffu, span, k2);
-			const float dx1 = __shfl_sync(0xffffffffu, dx, k1), ty1 = __shfl_sync(0xffffffffu, ty, k1);
-			const float dx2 = __shfl_sync(0xffffffffu, dx, k2), ty2 = __shfl_sync(0xffffffffu, ty, k2);
-			const uint32_t tri1 = __shfl_sync(0xffffffffu, tri, k1), tri2 = __shfl_sync(0xffffffffu, tri, k2);
-			const bool c1 = in_group && lane >= int(sp1 & 31u) && lane <= int(sp1 >> 5);
-			const bool c2 = two && in_group && lane >= int(sp2 & 31u) && lane <= int(sp2 >> 5);
-			const uint32_t key1 = nearFirstKey(dx1 * fx + ty1), key2 = nearFirstKey(dx2 * fx + ty2);
-			if(c1)
-				fn(t, key1, tri1);
-			if(c2)
-				fn(t, key2, tri2);
+			int k[4];
+			bool has[4];
+#pragma unroll
+			for(int u = 0; u < 4; u++) {
+				has[u] = todo != 0u;
+				k[u] = has[u] ? __ffs(todo) - 1 : 0;
+				if(has[u])
+					todo &= todo - 1u;
+			}
+			uint32_t sp[4], tr[4], key[4];
+			float kdx[4], kty[4];
+#pragma unroll
+			for(int u = 0; u < 4; u++) {
+				sp[u] = __shfl_sync(0xffffffffu, span, k[u]);
+				kdx[u] = __shfl_sync(0xffffffffu, dx, k[u]);
+				kty[u] = __shfl_sync(0xffffffffu, ty, k[u]);
+				tr[u] = __shfl_sync(0xffffffffu, tri, k[u]);
+			}
+#pragma unroll
+			for(int u = 0; u < 4; u++)
+				key[u] = nearFirstKey(kdx[u] * fx + kty[u]);
+#pragma unroll
+			for(int u = 0; u < 4; u++)
+				if(has[u] && in_group && lane >= int(sp[u] & 31u) && lane <= int(sp[u] >> 5))
+					fn(t, key[u], tr[u]);
 		}
 	}
 }
