@@ -49,7 +49,7 @@ constexpr int kWindow = 160;        // target fragments per pixel per depth wind
 // split its pixels' lists into small sub-segments (cheap thread sorts instead of warp sorts of
 // whole lists)
 constexpr int kHeavyPixel = 32;
-constexpr int kGroupBudget = 7168;  // sum over a group's pixels of min(count, kWindow)
+constexpr int kGroupBudget = 7680;  // sum over a group's pixels of min(count, kWindow)
 constexpr int kHistWords = 8192;    // per-group depth histogram (pixels x buckets)
 constexpr int kCoarseShift = 20;    // fragment estimate bins: depth keys >> 20 (4096 bins)
 constexpr int kCoarseBins = 1 << (32 - kCoarseShift);
