@@ -224,7 +224,7 @@ typedef struct lucid_options {
 	                               * demand, > 0 = fixed capacity, < 0 = none (the backward pass
 	                               * recomputes the fragment lists instead of reading them)      */
 	int32_t slab_fragments;    /* raster: fragments per unfinished pixel a depth slab aims at
-	                            * (0 = 210; a large value counts every key at once)            */
+	                            * (0 = 180; a large value counts every key at once)            */
 	int32_t reserved[3];
 } lucid_options;
 

@@ -184,7 +184,7 @@ void setShadingInputs(FrameParams& p, const lucid_frame_inputs* in) {
 }
 
 // fragments per unfinished pixel that a depth slab of the raster aims at
-int slabTarget(const lucid_renderer* r) { return r->opts.slab_fragments > 0 ? r->opts.slab_fragments : 210; }
+int slabTarget(const lucid_renderer* r) { return r->opts.slab_fragments > 0 ? r->opts.slab_fragments : 180; }
 
 FrameParams makeParams(lucid_renderer* r, const lucid_frame_inputs* in, float* out) {
 	FrameParams p{};

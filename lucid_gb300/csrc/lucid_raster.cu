@@ -844,7 +844,9 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 					atomicMin(&s.kmin, kmn);
 					atomicMax(&s.kmax, kmx);
 				}
-				nb_log = 31 - __clz(max(1, min(256, kHistWords / npix))); // buckets per pixel = 2^nb_log
+				// buckets per pixel = 2^nb_log, at most 128: finer buckets make the window walks
+				// longer than the sorts they save
+				nb_log = 31 - __clz(max(1, min(128, kHistWords / npix)));
 				// slabs of about p.slab_target fragments per unfinished pixel: slab k starts at the
 				// first estimate bin whose preceding fragments reach k times that (the bins'
 				// exclusive prefix sum, 8 bins per thread)

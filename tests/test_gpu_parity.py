@@ -153,7 +153,7 @@ def test_depth_windows_concentrated_depths(gpu, oracle):
     compare(sc, oracle)
 
 
-@pytest.mark.parametrize("slab", [8, 64, 210, 1 << 30])
+@pytest.mark.parametrize("slab", [8, 64, 180, 1 << 30])
 def test_depth_slabs(gpu, oracle, slab):
     """The per-pixel depth histograms built one key slab at a time (small slabs force many
     slabs per group, a huge one counts every key at once): same fragment lists and image."""
