@@ -106,7 +106,20 @@ def default_options() -> _lib.Options:
 
 
 class LucidRenderer:
-    """GB300 implementation of LucidRenderer's compute passes for one viewport size."""
+    """GB300 implementation of LucidRenderer's compute passes for one viewport size.
+
+    Keyword options map to `lucid_options` (0 or None keeps the library default):
+
+    * max_input_quads, max_visible_quads, max_bin_refs, band_capacity: buffer capacities;
+    * flags: LUCID_OPT_* bits (timers, additive, alpha threshold, pixel blend, reference order);
+    * low_high_threshold: tris per bin above which a bin is HIGH (work order);
+    * raster_ctas_per_sm, binning_ctas: launch shapes;
+    * max_views: views a batch may hold;
+    * grad_store_fragments: fragment store of the differentiable frame (0 grows on demand, < 0
+      none);
+    * slab_fragments: fragments per unfinished pixel that a depth slab of the raster's per-pixel
+      histograms aims at (0 = 180).
+    """
 
     def __init__(self, width: int, height: int, *, max_input_quads: int | None = None,
                  max_visible_quads: int | None = None, max_bin_refs: int | None = None,
