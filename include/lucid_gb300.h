@@ -184,7 +184,11 @@ typedef struct lucid_info {
 	uint64_t raster_windows;          /* depth windows processed by the raster pass         */
 	uint64_t raster_window_fragments; /* fragments sorted in those windows                  */
 	uint32_t raster_radix_windows;    /* windows sorted by the block-wide radix fallback    */
-	uint32_t ext_reserved[45];
+	uint32_t raster_light_bins;       /* bins rastered by the light path (<= 32 fragments
+	                                   * per pixel; one warp per row)                        */
+	uint64_t raster_blended_fragments;/* fragments blended: each pixel's fragments up to the
+	                                   * one that brings T to 0 (forward frames)             */
+	uint32_t ext_reserved[42];
 } lucid_info;
 
 #define LUCID_INFO_REFERENCE_WORDS 1152
@@ -370,6 +374,17 @@ lucid_status lucid_download_buffer(lucid_renderer* renderer, int32_t which, void
 lucid_status lucid_raster_dump(lucid_renderer* renderer, const lucid_frame_inputs* inputs,
 							   float* out_rgba, int32_t max_per_pixel, int32_t* host_counts,
 							   int32_t* host_prims, void* stream);
+
+/* The same verification mode for full-size frames: renders the whole frame into out_rgba and
+ * records the counts and first max_per_pixel prims of the pixels of the listed bins only
+ * (bins: HOST array of num_bins distinct bin ids, bin = by * bins_x + bx). Host outputs:
+ * host_counts[num_bins * 1024], host_prims[num_bins * 1024 * max_per_pixel]; bin k's local
+ * pixel (x, y) is entry k * 1024 + y * 32 + x (pixels outside the viewport read as count 0,
+ * prims -1; so do list entries past a pixel's count). Synchronous. Not in the reference-order mode. */
+lucid_status lucid_raster_dump_bins(lucid_renderer* renderer, const lucid_frame_inputs* inputs,
+									float* out_rgba, const int32_t* bins, int32_t num_bins,
+									int32_t max_per_pixel, int32_t* host_counts, int32_t* host_prims,
+									void* stream);
 
 /* Differentiable forward (no reference counterpart): lucid_render that also records each
  * pixel's colour accumulated in FP64 and keeps the frame's bin lists for lucid_render_backward.

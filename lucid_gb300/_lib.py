@@ -70,7 +70,8 @@ class Info(ctypes.Structure):
         ("num_fragments", c_uint64), ("num_hblock_tris", c_uint64),
         ("num_band_entries", c_uint32), ("num_views", c_uint32),
         ("raster_windows", c_uint64), ("raster_window_fragments", c_uint64),
-        ("raster_radix_windows", c_uint32), ("ext_reserved", c_uint32 * 45)]
+        ("raster_radix_windows", c_uint32), ("raster_light_bins", c_uint32),
+        ("raster_blended_fragments", ctypes.c_uint64), ("ext_reserved", c_uint32 * 42)]
 
 
 assert ctypes.sizeof(Info) == 1216 * 4
@@ -121,6 +122,8 @@ SIGNATURES = [
                                         ctypes.POINTER(c_size_t), c_void_p]),
     ("lucid_raster_dump", c_int32, [c_void_p, ctypes.POINTER(FrameInputsC), c_void_p, c_int32,
                                     c_void_p, c_void_p, c_void_p]),
+    ("lucid_raster_dump_bins", c_int32, [c_void_p, ctypes.POINTER(FrameInputsC), c_void_p, c_void_p,
+                                         c_int32, c_int32, c_void_p, c_void_p, c_void_p]),
     ("lucid_render_forward_grad", c_int32, [c_void_p, ctypes.POINTER(FrameInputsC), c_void_p, c_void_p]),
     ("lucid_render_backward", c_int32, [c_void_p, ctypes.POINTER(FrameInputsC), c_void_p,
                                         c_void_p, c_void_p, c_void_p]),

@@ -82,6 +82,7 @@ struct FrameParams {
 	int* dump_counts;     // verification mode (may be null)
 	int* dump_prims;
 	int dump_max;
+	const int* dump_bin_slot; // per bin: slot in the dump arrays, -1 = not recorded (null: all)
 	// gradient passes (kRasterStats / kRasterBackward)
 	double* px_color64;   // per pixel: FP64 unclamped colour (3 doubles, stats pass output)
 	float* px_color32;    // per pixel: FP32 unclamped colour (3 floats, clamp mask)

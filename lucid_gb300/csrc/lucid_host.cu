@@ -35,6 +35,7 @@ static_assert(offsetof(lucid_info, temp) == (LUCID_INFO_REFERENCE_WORDS - 64) * 
 static_assert(offsetof(lucid_info, error_code) == LUCID_INFO_REFERENCE_WORDS * 4, "LucidInfo layout");
 static_assert(sizeof(lucid_info) == LUCID_INFO_WORDS * 4, "lucid_info size");
 static_assert(offsetof(lucid_info, num_fragments) % 8 == 0, "64-bit counters alignment");
+static_assert(offsetof(lucid_info, raster_blended_fragments) % 8 == 0, "64-bit counters alignment");
 
 namespace {
 
@@ -252,7 +253,8 @@ lucid_status resetRasterCounters(lucid_renderer* r, cudaStream_t st) {
 	LUCID_CUDA_TRY(cudaMemsetAsync(&info->max_pixel_fragments, 0, 4, st));
 	LUCID_CUDA_TRY(cudaMemsetAsync(&info->num_fragments, 0, 16, st));
 	LUCID_CUDA_TRY(cudaMemsetAsync(info->raster_timers, 0, sizeof(info->raster_timers), st));
-	LUCID_CUDA_TRY(cudaMemsetAsync(&info->raster_windows, 0, 20, st));
+	LUCID_CUDA_TRY(cudaMemsetAsync(&info->raster_windows, 0,
+								   offsetof(lucid_info, ext_reserved) - offsetof(lucid_info, raster_windows), st));
 	return LUCID_OK;
 }
 
@@ -592,7 +594,8 @@ static lucid_status rasterPixelBlend(lucid_renderer* r, FrameParams p, cudaStrea
 }
 
 static lucid_status rasterImpl(lucid_renderer* r, const lucid_frame_inputs* in, float* out,
-							   int* dump_counts, int* dump_prims, int dump_max, cudaStream_t s) {
+							   int* dump_counts, int* dump_prims, int dump_max, cudaStream_t s,
+							   const int* dump_bin_slot = nullptr) {
 	if(!r || !r->have_frame)
 		return fail(LUCID_INVALID_ARG, "lucid_raster needs a prior lucid_quad_setup");
 	if(!out)
@@ -616,6 +619,7 @@ static lucid_status rasterImpl(lucid_renderer* r, const lucid_frame_inputs* in, 
 	p.dump_counts = dump_counts;
 	p.dump_prims = dump_prims;
 	p.dump_max = dump_max;
+	p.dump_bin_slot = dump_bin_slot;
 	if(r->opts.flags & LUCID_OPT_REFERENCE_ORDER) {
 		if(r->opts.flags & LUCID_OPT_ALPHA_THRESHOLD)
 			return fail(LUCID_NOT_SUPPORTED, "the reference-order mode has no alpha-threshold variant");
@@ -694,24 +698,51 @@ extern "C" lucid_status lucid_download_buffer(lucid_renderer* r, int32_t which, 
 	return LUCID_OK;
 }
 
-extern "C" lucid_status lucid_raster_dump(lucid_renderer* r, const lucid_frame_inputs* in, float* out,
-										  int32_t max_per_pixel, int32_t* host_counts,
-										  int32_t* host_prims, void* stream) {
+// Verification dump over the whole frame (bins == NULL) or over a subset of bins.
+static lucid_status rasterDump(lucid_renderer* r, const lucid_frame_inputs* in, float* out, int32_t max_per_pixel,
+							   const int32_t* bins, int32_t num_bins, int32_t* host_counts, int32_t* host_prims,
+							   void* stream) {
 	if(!r || !host_counts || max_per_pixel < 0 || (max_per_pixel > 0 && !host_prims))
 		return fail(LUCID_INVALID_ARG, "lucid_raster_dump: bad arguments");
-	cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-	const size_t npix = size_t(r->width) * r->height;
-	int *dc = nullptr, *dp = nullptr;
-	LUCID_CUDA_TRY(cudaMalloc(&dc, npix * 4));
-	if(max_per_pixel > 0) {
-		cudaError_t err = cudaMalloc(&dp, npix * max_per_pixel * 4);
-		if(err != cudaSuccess) {
-			cudaFree(dc);
-			return cudaFail(err, "cudaMalloc(dump)");
+	std::vector<int> slots;
+	if(bins && (r->opts.flags & LUCID_OPT_REFERENCE_ORDER))
+		return fail(LUCID_NOT_SUPPORTED, "lucid_raster_dump_bins: not in the reference-order mode");
+	if(bins) {
+		if(num_bins <= 0 || num_bins > r->bin_count)
+			return fail(LUCID_INVALID_ARG, "lucid_raster_dump_bins: num_bins out of range");
+		slots.assign(size_t(r->bin_count), -1);
+		for(int i = 0; i < num_bins; i++) {
+			if(bins[i] < 0 || bins[i] >= r->bin_count || slots[size_t(bins[i])] >= 0)
+				return fail(LUCID_INVALID_ARG, "lucid_raster_dump_bins: bin id out of range or repeated");
+			slots[size_t(bins[i])] = i;
 		}
-		cudaMemsetAsync(dp, 0xff, npix * max_per_pixel * 4, s);
 	}
-	cudaMemsetAsync(dc, 0, npix * 4, s);
+	cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+	const size_t npix = bins ? size_t(num_bins) * kBinSize * kBinSize : size_t(r->width) * r->height;
+	int *dc = nullptr, *dp = nullptr, *dslot = nullptr;
+	auto release = [&]() {
+		if(dc)
+			cudaFree(dc);
+		if(dp)
+			cudaFree(dp);
+		if(dslot)
+			cudaFree(dslot);
+	};
+	cudaError_t err = cudaMalloc(&dc, npix * 4);
+	if(err == cudaSuccess && max_per_pixel > 0)
+		err = cudaMalloc(&dp, npix * max_per_pixel * 4);
+	if(err == cudaSuccess && bins)
+		err = cudaMalloc(&dslot, slots.size() * 4);
+	if(err == cudaSuccess && bins)
+		err = cudaMemcpy(dslot, slots.data(), slots.size() * 4, cudaMemcpyHostToDevice);
+	if(err == cudaSuccess && dp)
+		err = cudaMemsetAsync(dp, 0xff, npix * max_per_pixel * 4, s);
+	if(err == cudaSuccess)
+		err = cudaMemsetAsync(dc, 0, npix * 4, s);
+	if(err != cudaSuccess) {
+		release();
+		return cudaFail(err, "lucid_raster_dump buffers");
+	}
 	lucid_status st = lucid_quad_setup(r, in, stream);
 	if(st == LUCID_OK)
 		st = lucid_bin_count(r, stream);
@@ -720,9 +751,9 @@ extern "C" lucid_status lucid_raster_dump(lucid_renderer* r, const lucid_frame_i
 	if(st == LUCID_OK)
 		st = lucid_bin_dispatch(r, stream);
 	if(st == LUCID_OK)
-		st = rasterImpl(r, in, out, dc, dp, max_per_pixel, s);
+		st = rasterImpl(r, in, out, dc, dp, max_per_pixel, s, dslot);
 	if(st == LUCID_OK) {
-		cudaError_t err = cudaStreamSynchronize(s);
+		err = cudaStreamSynchronize(s);
 		if(err == cudaSuccess)
 			err = cudaMemcpy(host_counts, dc, npix * 4, cudaMemcpyDeviceToHost);
 		if(err == cudaSuccess && dp)
@@ -730,10 +761,22 @@ extern "C" lucid_status lucid_raster_dump(lucid_renderer* r, const lucid_frame_i
 		if(err != cudaSuccess)
 			st = cudaFail(err, "lucid_raster_dump readback");
 	}
-	cudaFree(dc);
-	if(dp)
-		cudaFree(dp);
+	release();
 	return st;
+}
+
+extern "C" lucid_status lucid_raster_dump(lucid_renderer* r, const lucid_frame_inputs* in, float* out,
+										  int32_t max_per_pixel, int32_t* host_counts,
+										  int32_t* host_prims, void* stream) {
+	return rasterDump(r, in, out, max_per_pixel, nullptr, 0, host_counts, host_prims, stream);
+}
+
+extern "C" lucid_status lucid_raster_dump_bins(lucid_renderer* r, const lucid_frame_inputs* in, float* out,
+											   const int32_t* bins, int32_t num_bins, int32_t max_per_pixel,
+											   int32_t* host_counts, int32_t* host_prims, void* stream) {
+	if(!bins)
+		return fail(LUCID_INVALID_ARG, "lucid_raster_dump_bins: bins is NULL");
+	return rasterDump(r, in, out, max_per_pixel, bins, num_bins, host_counts, host_prims, stream);
 }
 
 // Per-pixel offsets / counts and the state words of the fragment store (allocated once).

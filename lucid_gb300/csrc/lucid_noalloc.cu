@@ -131,8 +131,14 @@ extern "C" lucid_status lucid_bin_noalloc(const uint32_t* quad_aabbs, const uint
 	launchBinCount(p, s);
 	launchBinCategorize(p, s);
 	launchBinDispatch(p, s);
-	if(info_out)
-		cudaMemcpyAsync(info_out, info, sizeof(lucid_info), cudaMemcpyDeviceToDevice, s);
+	if(info_out) {
+		err = cudaMemcpyAsync(info_out, info, sizeof(lucid_info), cudaMemcpyDeviceToDevice, s);
+		if(err != cudaSuccess) {
+			cudaGetLastError();
+			return noallocFail(LUCID_CUDA_ERROR, std::string("lucid_bin_noalloc: copy to info_out: ") +
+													 cudaGetErrorString(err));
+		}
+	}
 	err = cudaGetLastError();
 	if(err != cudaSuccess)
 		return noallocFail(LUCID_CUDA_ERROR, std::string("lucid_bin_noalloc launch: ") + cudaGetErrorString(err));

@@ -54,6 +54,10 @@ constexpr int kHistWords = 8192;    // per-group depth histogram (pixels x bucke
 constexpr int kCoarseShift = 20;    // fragment estimate bins: depth keys >> 20 (4096 bins)
 constexpr int kCoarseBins = 1 << (32 - kCoarseShift);
 constexpr int kMaxSlabs = 64;       // depth slabs of one group at most
+// light bins: at most kLightPixel fragments per pixel, so one row's fragments fit a warp's
+// kLightPool-entry slice of the sort buffers
+constexpr int kLightPixel = 32;
+constexpr int kLightPool = 32 * kLightPixel;
 
 struct RasterSmem {
 	// kv[b][0] = keys, kv[b][1] = payloads of buffer b; the buffer not holding the sorted
@@ -98,6 +102,7 @@ struct RasterSmem {
 	int group_end;
 	int single_digit;
 	int any_big;
+	int bin_maxpx;   // most fragments of one pixel of the bin
 	int view;        // view of the current bin (batched frames)
 	int loaded_view; // view whose parameters view_params holds
 	int store_ok;    // kRasterStore: the bin's fragments fit the store
@@ -106,6 +111,7 @@ struct RasterSmem {
 
 static_assert(sizeof(RasterSmem) <= 227 * 1024, "raster shared memory exceeds one SM");
 static_assert(256 * NW == kGroupCap / 2, "the small sub-segment lists share the radix histograms' size");
+static_assert(2 * NW * kLightPool <= 4 * kGroupCap, "the light path's row pools live in the sort buffers");
 
 // Depth histogram slot of pixel t's bucket bk (2^nb_log >= 32 buckets per pixel). The bucket is
 // XOR-swizzled by the pixel's lane so that the 32 pixels of a row, which mostly hit the same
@@ -130,6 +136,18 @@ __device__ __forceinline__ uint32_t entryTri(uint2 e) { return (e.x >> 20) | ((e
 // tri field).
 __device__ __forceinline__ uint32_t fragPayload(int tp, uint32_t tri) { return uint32_t(tp) | (tri << 8); }
 __device__ __forceinline__ uint32_t payloadTri(uint32_t val) { return val >> 8; }
+
+// Verification dump: index of pixel (px, py), local pixel pl of `bin`, in the dump arrays, or
+// -1 when it is not recorded. Whole frame: y * width + x; bin subset: slot * 1024 + pl.
+__device__ __forceinline__ long long dumpPixel(const FrameParams& p, int bin, int pl, int px, int py) {
+	if(px >= p.width || py >= p.height)
+		return -1;
+	if(p.dump_bin_slot) {
+		const int slot = p.dump_bin_slot[bin];
+		return slot < 0 ? -1 : (long long)slot * 1024 + pl;
+	}
+	return (long long)py * p.width + px;
+}
 
 __device__ __forceinline__ uint32_t fragPrim(const FrameParams& p, uint32_t val) {
 	const uint32_t tri = payloadTri(val);
@@ -431,6 +449,133 @@ __device__ __forceinline__ void forEachGroupFragment(const FrameParams& p, const
 	}
 }
 
+// Input primitive id of a tri slot (ties between equal depth keys go by it).
+__device__ __forceinline__ uint32_t triPrim(const FrameParams& p, uint32_t tri) {
+	return __ldg(p.quad_source + (tri >> 1)) * 2 + (tri & 1);
+}
+
+// One row of a light bin, by one warp (lane = pixel column): every fragment of the row goes
+// into the warp's pool (K: depth keys, V: tri slots), the lane's pixel at [off, off + count);
+// then each lane blends its pixel front to back, taking the nearest remaining fragment (ties by
+// input primitive id) each step, and stops once T == 0: nothing behind that point is ordered or
+// shaded. The keys, shading and blend are the FP32 expressions of the group path
+// (shading.glsl:116, :279-280, :312). Returns the fragments the lane blended.
+__device__ unsigned long long lightRow(const FrameParams& p, const RasterSmem& s, const uint2* scratch,
+									   const float4* planes, int band_cap, int bin, int bin_x, int bin_y, int row,
+									   uint32_t* K, uint32_t* V, float4 bg, bool additive, bool alpha_threshold,
+									   bool dump) {
+	const int lane = threadIdx.x & 31;
+	const int pl = row * 32 + lane;
+	const int cnt = s.pix_count[pl];
+	const int off = warpInclusiveScan(cnt) - cnt;
+	const int px = bin_x + lane, py = bin_y + row;
+	// A. the row's fragments from the band entries (spans already clipped to the viewport)
+	int cur = off;
+	const int end = off + cnt;
+	if(__any_sync(0xffffffffu, cnt > 0)) {
+		const int b = row >> 2, rshift = 5 * (row & 3);
+		const int ne = s.band_count[b];
+		const float fx = float(px), fy = float(py);
+		for(int j0 = 0; j0 < ne; j0 += 32) {
+			const int j = j0 + lane;
+			bool rel = j < ne;
+			uint32_t span = 0u, tri = 0u;
+			float dx = 0.0f, ty = 0.0f;
+			if(rel) {
+				const uint2 e = scratch[size_t(b) * band_cap + j];
+				const int lo = (e.x >> rshift) & 31, hi = (e.y >> rshift) & 31;
+				rel = lo <= hi;
+				if(rel) {
+					const float4 d = planes[size_t(b) * band_cap + j];
+					tri = entryTri(e);
+					dx = d.x;
+					ty = d.y * fy + d.z;
+					span = uint32_t(lo) | uint32_t(hi) << 5;
+				}
+			}
+			uint32_t todo = __ballot_sync(0xffffffffu, rel);
+			while(todo != 0u) {
+				int k[4];
+				bool has[4];
+#pragma unroll
+				for(int u = 0; u < 4; u++) {
+					has[u] = todo != 0u;
+					k[u] = has[u] ? __ffs(todo) - 1 : 0;
+					if(has[u])
+						todo &= todo - 1u;
+				}
+				uint32_t sp[4], tr[4];
+				float kdx[4], kty[4];
+#pragma unroll
+				for(int u = 0; u < 4; u++) {
+					sp[u] = __shfl_sync(0xffffffffu, span, k[u]);
+					kdx[u] = __shfl_sync(0xffffffffu, dx, k[u]);
+					kty[u] = __shfl_sync(0xffffffffu, ty, k[u]);
+					tr[u] = __shfl_sync(0xffffffffu, tri, k[u]);
+				}
+#pragma unroll
+				for(int u = 0; u < 4; u++)
+					if(has[u] && lane >= int(sp[u] & 31u) && lane <= int(sp[u] >> 5)) {
+						if(cur < end) {
+							K[cur] = nearFirstKey(kdx[u] * fx + kty[u]);
+							V[cur] = tr[u];
+						}
+						cur++;
+					}
+			}
+		}
+	}
+	__syncwarp();
+	if(cur != end)
+		raiseError(p.info, LUCID_ERR_BIN_COUNT, uint32_t(bin), uint32_t(pl), uint32_t(cur - off));
+	// B. front-to-back blend by selection
+	float T = 1.0f, c0 = 0.0f, c1 = 0.0f, c2 = 0.0f;
+	int n = min(cur, end) - off, k = 0;
+	long long dbase = dump ? dumpPixel(p, bin, pl, px, py) : -1;
+	while(n > 0) {
+		if(!additive && !dump && T == 0.0f)
+			break;
+		int bi = off;
+		uint32_t bk = K[off];
+		for(int i = off + 1; i < off + n; i++) {
+			const uint32_t ki = K[i];
+			if(ki < bk || (ki == bk && triPrim(p, V[i]) < triPrim(p, V[bi])))
+				bi = i, bk = ki;
+		}
+		const uint32_t tri = V[bi];
+		K[bi] = K[off + n - 1];
+		V[bi] = V[off + n - 1];
+		n--;
+		const float4 c = shadeFragment(p, tri, keyToDepth(bk), px, py);
+		if(dbase >= 0 && k < p.dump_max)
+			p.dump_prims[size_t(dbase) * p.dump_max + k] = int(triPrim(p, tri));
+		k++;
+		const float qx = c.x * c.w, qy = c.y * c.w, qz = c.z * c.w;
+		if(additive) {
+			c0 = c0 + qx;
+			c1 = c1 + qy;
+			c2 = c2 + qz;
+		} else {
+			c0 = c0 + qx * T;
+			c1 = c1 + qy * T;
+			c2 = c2 + qz * T;
+			T = T * (1.0f - c.w);
+			if(alpha_threshold && T < (1.0f / 128.0f))
+				break;
+		}
+	}
+	float4 o;
+	o.x = fminf(fmaxf(c0 + T * bg.x, 0.0f), 1.0f);
+	o.y = fminf(fmaxf(c1 + T * bg.y, 0.0f), 1.0f);
+	o.z = fminf(fmaxf(c2 + T * bg.z, 0.0f), 1.0f);
+	o.w = 1.0f;
+	writePixel(p, px, py, o);
+	if(dbase >= 0)
+		p.dump_counts[dbase] = cnt;
+	__syncwarp();
+	return (unsigned long long)k;
+}
+
 // Work sources of the raster kernel: the bins of one frame, or the bins of every view of a
 // batched frame.
 struct OneViewWork {
@@ -542,6 +687,7 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 		if(tid == 0) {
 			work.next(s);
 			s.stat_hbt = 0;
+			s.bin_maxpx = 0;
 		}
 		if(tid < 8)
 			s.band_count[tid] = 0;
@@ -697,8 +843,10 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 #pragma unroll
 			for(int o = 16; o > 0; o >>= 1)
 				mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-			if(lane == 0 && mx > 0)
+			if(lane == 0 && mx > 0) {
 				atomicMax(&p.info->max_pixel_fragments, uint32_t(mx));
+				atomicMax(&s.bin_maxpx, mx);
+			}
 			if(tid == 0) {
 				unsigned long long hb = s.stat_hbt;
 				atomicAdd((unsigned long long*)&p.info->num_fragments, (unsigned long long)frags);
@@ -710,8 +858,32 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 		__syncthreads();
 		RASTER_TIMER(1);
 
+		// ---- L. light bins (every pixel has at most kLightPixel fragments): one warp per row,
+		// no CTA barrier until the bin is done
+		if constexpr(MODE == kRasterForward) {
+			if(s.bin_maxpx <= kLightPixel) {
+				uint32_t* K = &s.kv[0][0][0] + warp * kLightPool;
+				uint32_t* V = &s.kv[0][0][0] + NW * kLightPool + warp * kLightPool;
+				unsigned long long blended = 0;
+				for(int row = warp; row < 32; row += NW)
+					blended += lightRow(p, s, scratch, planes, band_cap, bin, bin_x, bin_y, row, K, V, bg, additive,
+										alpha_threshold, dump);
+#pragma unroll
+				for(int o = 16; o > 0; o >>= 1)
+					blended += __shfl_xor_sync(0xffffffffu, blended, o);
+				if(lane == 0 && blended)
+					atomicAdd((unsigned long long*)&p.info->raster_blended_fragments, blended);
+				if(tid == 0)
+					atomicAdd(&p.info->raster_light_bins, 1u);
+				__syncthreads();
+				RASTER_TIMER(3);
+				continue;
+			}
+		}
+
 		// ---- C. pixel groups
 		int p0 = 0;
+		unsigned long long nblend = 0; // fragments this thread's pixels blended (forward mode)
 		while(p0 < 1024) {
 			if(tid == 0) {
 				int base = s.eff_prefix[p0];
@@ -1426,10 +1598,9 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 								int idx = s.px_done[t] + (f - fbeg);
 								if(idx < p.dump_max) {
 									int pl = p0 + t;
-									int px = bin_x + (pl & 31), py = bin_y + (pl >> 5);
-									if(px < p.width && py < p.height)
-										p.dump_prims[(size_t(py) * p.width + px) * p.dump_max + idx] =
-											int(fragPrim(p, V[f]));
+									long long di = dumpPixel(p, bin, pl, bin_x + (pl & 31), bin_y + (pl >> 5));
+									if(di >= 0)
+										p.dump_prims[size_t(di) * p.dump_max + idx] = int(fragPrim(p, V[f]));
 								}
 							}
 							if constexpr(MODE == kRasterForward) {
@@ -1465,6 +1636,8 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 								}
 							}
 						}
+						if constexpr(MODE == kRasterForward)
+							nblend += (unsigned long long)(f - s.px_bcur[t]);
 						s.px_bcur[t] = f;
 						s.px_T[t] = T;
 						s.px_c[t][0] = c0, s.px_c[t][1] = c1, s.px_c[t][2] = c2;
@@ -1514,8 +1687,11 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 				o.z = fminf(fmaxf(un[2], 0.0f), 1.0f);
 				o.w = 1.0f;
 				writePixel(p, px, py, o);
-				if(dump && px < p.width && py < p.height)
-					p.dump_counts[size_t(py) * p.width + px] = s.pix_count[pl];
+				if(dump) {
+					long long di = dumpPixel(p, bin, pl, px, py);
+					if(di >= 0)
+						p.dump_counts[di] = s.pix_count[pl];
+				}
 				if constexpr(MODE == kRasterStats) {
 					if(px < p.width && py < p.height) {
 						size_t pix = size_t(py) * p.width + px;
@@ -1529,6 +1705,13 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 			__syncthreads();
 			RASTER_TIMER(7);
 			p0 = p1;
+		}
+		if constexpr(MODE == kRasterForward) {
+#pragma unroll
+			for(int o = 16; o > 0; o >>= 1)
+				nblend += __shfl_xor_sync(0xffffffffu, nblend, o);
+			if(lane == 0 && nblend)
+				atomicAdd((unsigned long long*)&p.info->raster_blended_fragments, nblend);
 		}
 	}
 	if(timers && tid == 0)

@@ -217,6 +217,21 @@ class LucidRenderer:
               "lucid_raster_dump")
         return out, counts, prims[..., :max_per_pixel]
 
+    def raster_dump_bins(self, frame: FrameInputs, bins, max_per_pixel: int, stream=None):
+        """Full frame, recording the fragment lists of the listed bins only: (image, counts
+        [n, 32, 32], prims [n, 32, 32, max_per_pixel]) with bin k's pixel (x, y) at [k, y, x]
+        (pixels outside the viewport stay 0 / -1)."""
+        out = self.new_image()
+        b = np.ascontiguousarray(bins, np.int32)
+        counts = np.zeros((len(b), 32, 32), np.int32)
+        prims = np.zeros((len(b), 32, 32, max(1, max_per_pixel)), np.int32)
+        fi = frame.c_struct()
+        check(self.lib.lucid_raster_dump_bins(self.handle, ctypes.byref(fi), _dptr(out), b.ctypes.data, len(b),
+                                              max_per_pixel, counts.ctypes.data, prims.ctypes.data,
+                                              _stream_ptr(stream)),
+              "lucid_raster_dump_bins")
+        return out, counts, prims[..., :max_per_pixel]
+
     # -- info / statistics ------------------------------------------------------------------
     def autotune(self, frame: FrameInputs, stream=None) -> dict:
         """Runs lucid_autotune on `frame`; the winner stays in the renderer."""

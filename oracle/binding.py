@@ -53,6 +53,7 @@ class OracleOutputs(ctypes.Structure):
         ("max_per_pixel", ctypes.c_int32),
         ("num_fragments", ctypes.c_uint64), ("num_hblock_tris", ctypes.c_uint64),
         ("max_pixel_fragments", ctypes.c_uint32), ("invalid_pixels", ctypes.c_uint64),
+        ("dump_by_subset", ctypes.c_int32),
     ]
 
 
@@ -101,8 +102,13 @@ def _shading_inputs(scene, keep):
 
 def run(scene, max_visible_quads: int | None = None, raster: bool = True, image64: bool = False,
         bin_subset=None, threads: int = 1, max_per_pixel: int = 0, flags: int = 0,
-        low_high_threshold: int = 1024, setup_outputs: bool = True, order_mode: int = 0):
-    """Runs the oracle on a ``lucid_gb300.scenes.Scene``; returns a dict of numpy arrays."""
+        low_high_threshold: int = 1024, setup_outputs: bool = True, order_mode: int = 0,
+        dump_by_subset: bool = False):
+    """Runs the oracle on a ``lucid_gb300.scenes.Scene``; returns a dict of numpy arrays.
+
+    With ``bin_subset`` and ``dump_by_subset`` (exact order only) the fragment counts and
+    prims cover the subset's bins alone, in ascending bin order: ``frag_counts`` [n, 32, 32],
+    ``frag_prims`` [n, 32, 32, max_per_pixel]; the images stay full-frame."""
     L = lib()
     mvq = max_visible_quads or max(1024, scene.num_quads)
     w, h = scene.width, scene.height
@@ -130,13 +136,15 @@ def run(scene, max_visible_quads: int | None = None, raster: bool = True, image6
     cap = int(8 * scene.num_quads + 1024)
     out["bin_quads"] = np.zeros(cap, np.uint32)
     out["bin_tris"] = np.zeros(cap, np.uint32)
+    compact = dump_by_subset and subset is not None and order_mode == 0
     if raster:
         out["image"] = np.zeros((h, w, 4), np.float32)
-        out["frag_counts"] = np.zeros((h, w), np.int32)
+        dump_shape = (len(subset), 32, 32) if compact else (h, w)
+        out["frag_counts"] = np.zeros(dump_shape, np.int32)
         if image64:
             out["image64"] = np.zeros((h, w, 4), np.float64)
         if max_per_pixel > 0:
-            out["frag_prims"] = np.full((h, w, max_per_pixel), -1, np.int32)
+            out["frag_prims"] = np.full(dump_shape + (max_per_pixel,), -1, np.int32)
 
     cfg = scene.config
     keep = []
@@ -154,6 +162,7 @@ def run(scene, max_visible_quads: int | None = None, raster: bool = True, image6
         setattr(outs, k, v.ctypes.data)
     outs.bin_refs_capacity = cap
     outs.max_per_pixel = max_per_pixel
+    outs.dump_by_subset = 1 if compact else 0
     rc = L.oracle_run(ctypes.byref(ins), ctypes.byref(outs))
     if rc != 0:
         raise RuntimeError(f"oracle_run failed ({rc})")

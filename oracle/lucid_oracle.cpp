@@ -889,7 +889,7 @@ inline bool fragLess(const Frag& a, const Frag& b) {
 	return a.key != b.key ? a.key < b.key : a.prim < b.prim;
 }
 
-void rasterBin(const State& s, int bin, oracle_outputs* out, std::vector<std::vector<Frag>>& px,
+void rasterBin(const State& s, int bin, int slot, oracle_outputs* out, std::vector<std::vector<Frag>>& px,
 			   uint64_t& nfrag, uint64_t& nhbt, uint32_t& maxfrag) {
 	const oracle_inputs* in = s.in;
 	int bx = bin % s.bcx, by = bin / s.bcx;
@@ -898,6 +898,7 @@ void rasterBin(const State& s, int bin, oracle_outputs* out, std::vector<std::ve
 	const float* bg = in->config->background_color;
 	bool additive = (in->flags & LUCID_OPT_ADDITIVE_BLENDING) != 0;
 	bool alpha_threshold = (in->flags & LUCID_OPT_ALPHA_THRESHOLD) != 0;
+	const bool img64_requested = out->image64 != nullptr;
 	for(int r = 0; r < 32; r++) {
 		int py = bin_y + r;
 		if(py >= s.h)
@@ -911,31 +912,41 @@ void rasterBin(const State& s, int bin, oracle_outputs* out, std::vector<std::ve
 			nfrag += fr.size();
 			maxfrag = std::max(maxfrag, uint32_t(fr.size()));
 			size_t pix = size_t(py) * s.w + pxx;
+			// dump index: the whole frame, or (dump_by_subset) the bin's slot in the subset
+			const size_t dpix = out->dump_by_subset ? size_t(slot) * 1024 + size_t(r * 32 + x) : pix;
 			if(out->frag_counts)
-				out->frag_counts[pix] = int32_t(fr.size());
+				out->frag_counts[dpix] = int32_t(fr.size());
 			if(out->frag_prims) {
-				int32_t* dst = out->frag_prims + pix * out->max_per_pixel;
+				int32_t* dst = out->frag_prims + dpix * out->max_per_pixel;
 				for(int i = 0; i < out->max_per_pixel; i++)
 					dst[i] = i < int(fr.size()) ? int32_t(fr[i].prim) : -1;
 			}
-			// shading.glsl:279-280,312 in FP32 (and FP64 over the same FP32 colours)
+			// shading.glsl:279-280,312 in FP32 (and, when image64 is requested, FP64 over the
+			// same FP32 colours). Without image64 the FP32 loop stops once T == 0: every later
+			// fragment would add (c * a) * 0 = 0 and keep T at 0.
+			const bool want64 = img64_requested;
 			float oc[3] = {0.0f, 0.0f, 0.0f}, T = 1.0f;
 			double oc64[3] = {0.0, 0.0, 0.0}, T64 = 1.0;
 			for(const Frag& f : fr) {
+				if(!want64 && !additive && T == 0.0f)
+					break;
 				float c[4];
 				shadeFragment(s, f, pxx, py, c);
 				if(additive) {
-					for(int j = 0; j < 3; j++) {
+					for(int j = 0; j < 3; j++)
 						oc[j] = oc[j] + c[j] * c[3];
-						oc64[j] = oc64[j] + double(c[j]) * double(c[3]);
-					}
+					if(want64)
+						for(int j = 0; j < 3; j++)
+							oc64[j] = oc64[j] + double(c[j]) * double(c[3]);
 				} else {
-					for(int j = 0; j < 3; j++) {
+					for(int j = 0; j < 3; j++)
 						oc[j] = oc[j] + (c[j] * c[3]) * T;
-						oc64[j] = oc64[j] + (double(c[j]) * double(c[3])) * T64;
-					}
 					T = T * (1.0f - c[3]);
-					T64 = T64 * (1.0 - double(c[3]));
+					if(want64) {
+						for(int j = 0; j < 3; j++)
+							oc64[j] = oc64[j] + (double(c[j]) * double(c[3])) * T64;
+						T64 = T64 * (1.0 - double(c[3]));
+					}
 					if(alpha_threshold && T < (1.0f / 128.0f))
 						break;
 				}
@@ -1462,7 +1473,7 @@ void raster(State& s, oracle_outputs* out) {
 			if(in->order_mode == 1)
 				rasterBinRef(s, bins[i], out, nf[tid], nh[tid], mf[tid], ni[tid]);
 			else
-				rasterBin(s, bins[i], out, px, nf[tid], nh[tid], mf[tid]);
+				rasterBin(s, bins[i], int(i), out, px, nf[tid], nh[tid], mf[tid]);
 		}
 	};
 	if(nt == 1)

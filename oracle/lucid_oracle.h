@@ -88,6 +88,9 @@ typedef struct oracle_outputs {
 	uint64_t num_hblock_tris;
 	uint32_t max_pixel_fragments;
 	uint64_t invalid_pixels; /* reference-order mode: pixels whose window overflowed */
+	/* exact mode with bin_subset: frag_counts / frag_prims hold only the subset's bins, bin k
+	 * of the subset at [k * 1024 + local pixel] (image and image64 stay full-frame)   */
+	int32_t dump_by_subset;
 } oracle_outputs;
 
 /* Runs setup, binning and (if out->image or out->frag_counts is set) the raster pass.

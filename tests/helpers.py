@@ -68,3 +68,14 @@ def used_slots(nvis, mvq):
     small = np.arange(nvis[0])
     large = mvq - 1 - np.arange(nvis[1])
     return np.concatenate([small, large]).astype(np.int64)
+
+
+def assert_bin_lists_equal(counters, bin_count, bin_quads, bin_tris, ref_counters, ref_quads, ref_tris):
+    """Per-bin quad and tri reference lists of two binning runs are the same lists."""
+    gq = canonical_quad_lists(counters, bin_count, bin_quads)
+    rq = canonical_quad_lists(ref_counters, bin_count, ref_quads)
+    gt = canonical_tri_lists(counters, bin_count, bin_tris)
+    rt = canonical_tri_lists(ref_counters, bin_count, ref_tris)
+    for b in range(bin_count):
+        np.testing.assert_array_equal(gq[b], rq[b], err_msg=f"bin {b} quads")
+        np.testing.assert_array_equal(gt[b], rt[b], err_msg=f"bin {b} tris")

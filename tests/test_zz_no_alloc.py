@@ -88,6 +88,43 @@ def test_no_alloc_binning_matches_regular_path_twice(gpu, lucid_lib):
         check_same(ref, counters, bq, bt, info, bins)
 
 
+def test_no_alloc_reference_overflow_keeps_writes_in_bounds(gpu, lucid_lib):
+    """Too small a max_bin_refs: the call still succeeds, info_out reports LUCID_ERR_BIN_REFS,
+    and no reference is written past max_bin_refs (sentinels behind the lists stay intact)."""
+    import torch
+    from lucid_gb300 import _lib
+    mvq, cap, pad = 8192, 300, 4096
+    sc = scenes.random_tris(640, 360, 5000, seed=33, area_median=300.0, area_sigma=1.2,
+                            large_fraction=0.03, large_area=(2000.0, 20000.0))
+    ref = regular_binning(sc, mvq, 1 << 17)
+    info = ref["info"]
+    assert int(info.num_bin_quad_refs) > cap and int(info.num_bin_tri_refs) > cap
+    bins = ((sc.width + 31) // 32) * ((sc.height + 31) // 32)
+    sentinel = 0x5A5A5A5A
+    d_aabbs = torch.from_numpy(ref["aabbs"].view(np.int32)).cuda()
+    d_scan = torch.from_numpy(ref["scan"].view(np.int32)).cuda()
+    d_counters = torch.zeros((10 * bins,), dtype=torch.int32, device="cuda")
+    d_bq = torch.full((cap + pad,), sentinel, dtype=torch.int32, device="cuda")
+    d_bt = torch.full((cap + pad,), sentinel, dtype=torch.int32, device="cuda")
+    d_info = torch.zeros((ctypes.sizeof(_lib.Info) // 4,), dtype=torch.int32, device="cuda")
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    st = lucid_lib.lucid_bin_noalloc(d_aabbs.data_ptr(), d_scan.data_ptr(), info.num_visible_quads[0],
+                                     info.num_visible_quads[1], mvq, sc.width, sc.height, 1024,
+                                     d_counters.data_ptr(), d_bq.data_ptr(), d_bt.data_ptr(), cap,
+                                     d_info.data_ptr(), stream)
+    assert st == 0, lucid_lib.lucid_last_error_string()
+    torch.cuda.synchronize()
+    out_info = _lib.Info.from_buffer_copy(d_info.cpu().numpy().tobytes())
+    assert out_info.error_code == 2  # LUCID_ERR_BIN_REFS
+    bq, bt = d_bq.cpu().numpy(), d_bt.cpu().numpy()
+    assert (bq[cap:] == sentinel).all() and (bt[cap:] == sentinel).all()
+    assert (bq[:cap] != sentinel).any() and (bt[:cap] != sentinel).any()
+    # counts and offsets are still complete: they do not depend on the list capacity
+    counters = d_counters.cpu().numpy().view(np.uint32)
+    np.testing.assert_array_equal(counters[:2 * bins], ref["counters"][:2 * bins])
+    np.testing.assert_array_equal(counters[3 * bins:5 * bins], ref["counters"][3 * bins:5 * bins])
+
+
 def test_no_alloc_rejects_oversized_viewport(gpu, lucid_lib):
     from lucid_gb300 import _lib
     st = lucid_lib.lucid_bin_noalloc(None, None, 0, 0, 1024, 3840, 2160, 1024, None, None, None, 0,
