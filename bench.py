@@ -10,8 +10,13 @@ value      fragments/s with the scene resident in device memory (CUDA events aro
 e2e        same metric through lucid_render with host buffers: every step copies the scene from
            pinned host memory and reads the FP32 image back.
 roofline   raster kernel (the dominant kernel): algorithmic bytes per launch / its measured time.
-cpu_baseline  the CPU oracle (port of the reference passes), all host threads, on a seeded
-           sample of bins; its frame time is extrapolated from the sample's fragments.
+cpu_baseline  the CPU oracle (port of the reference passes): one whole frame of the workload on
+           all host threads (measured), and the 1280x720 / 100k-triangle frame on 1 core and on
+           all cores.
+parity     (not timed) the benchmark frame against the oracle on 16 seeded bins: fragment order
+           bit-exact, image error, and the FP32 image's error against the FP64 blend.
+workloads  the 3840x2160 / 5M-triangle mesh frame and the 1280x720 / 100k-triangle frame: frame
+           time, fragments/s and the time of each pass.
 
 --impl reference runs the CPU oracle only (the reference itself runs only as Vulkan GLSL).
 Multi-GPU (torchrun): independent replicas, one frame per rank per step ("scaling": "weak").
@@ -147,42 +152,112 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(scene, sample_bins, seed=0):
-    """Times the CPU oracle on all host threads: setup + binning on the whole scene, raster on a
-    seeded sample of bins; the raster time is extrapolated by the fraction of fragments."""
+def cpu_frame(scene, threads):
+    """One whole frame of the CPU oracle (setup, binning, raster of every bin, FP32 blend that
+    stops at T == 0): wall time in seconds and the frame's fragments."""
     from oracle import binding
-    threads = os.cpu_count() or 1
+    mvq = max(1024, scene.num_quads)
+    t0 = time.perf_counter()
+    o = binding.run(scene, max_visible_quads=mvq, raster=True, threads=threads, setup_outputs=False)
+    return time.perf_counter() - t0, int(o["num_fragments"])
+
+
+def cpu_sample(scene, sample_bins, threads, seed=0):
+    """The CPU oracle on a seeded sample of bins (setup and binning of the whole frame, raster of
+    `sample_bins` random bins); the raster time is extrapolated to the frame by fragments."""
+    from oracle import binding
     mvq = max(1024, scene.num_quads)
     t0 = time.perf_counter()
     full = binding.run(scene, max_visible_quads=mvq, raster=False, setup_outputs=False)
     t_bin = time.perf_counter() - t0
     n = full["bin_count"]
-    c = full["bin_counters"]
     rng = np.random.default_rng(seed)
     k = min(n, sample_bins)
     subset = np.sort(rng.choice(n, size=k, replace=False)).astype(np.int32)
     t0 = time.perf_counter()
-    part = binding.run(scene, max_visible_quads=mvq, raster=True, bin_subset=subset,
-                       threads=threads, setup_outputs=False)
-    t_all = time.perf_counter() - t0
-    t_raster = max(t_all - t_bin, 1e-9)  # the sampled run repeats setup + binning
-    frag_sample = part["num_fragments"]
-    return dict(t_bin=t_bin, t_raster_sample=t_raster, frag_sample=frag_sample, bins=k,
-                bin_count=n, threads=threads,
-                tris_per_bin_sample=int((2 * c[:n][subset] + c[3 * n:4 * n][subset]).sum()))
+    part = binding.run(scene, max_visible_quads=mvq, raster=True, bin_subset=subset, threads=threads,
+                       setup_outputs=False)
+    t_raster = max(time.perf_counter() - t0 - t_bin, 1e-9)  # the sampled run repeats setup + binning
+    return dict(t_bin=t_bin, t_raster_sample=t_raster, frag_sample=int(part["num_fragments"]), bins=k,
+                bin_count=n)
+
+
+def host_cores():
+    return os.cpu_count() or 1
+
+
+def cpu_baselines(scene, fragments):
+    """Rank 0 at N=1: the oracle's whole benchmark frame on all host cores (measured, not
+    extrapolated) and the 1280x720 / 100k-triangle frame on 1 core and on all cores."""
+    from lucid_gb300 import scenes
+    cores = host_cores()
+    t_frame, frags = cpu_frame(scene, cores)
+    assert frags == fragments, (frags, fragments)
+    c0 = scenes.workload("cpu720")
+    t1, f0 = cpu_frame(c0, 1)
+    tn, _ = cpu_frame(c0, cores)
+    return {"value": frags / t_frame, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": (f"one whole frame of the workload by the oracle (setup, binning, every bin's raster; "
+                       f"FP32 blend stopping at T == 0) on {cores} host threads"),
+            "ms_per_frame": t_frame * 1e3,
+            "cpu720": {"workload": "1280x720, 100k random triangles", "fragments": f0,
+                       "ms_per_frame_1_core": t1 * 1e3, "ms_per_frame_all_cores": tn * 1e3, "cores": cores}}
+
+
+def parity_sample(r, frame, scene, num_bins=16, max_per_pixel=64, seed=0):
+    """Checks the benchmark frame against the oracle on a seeded sample of bins (not timed):
+    per-pixel fragment counts and first fragments in blend order bit-exact, image within 1e-5,
+    and the FP32 image's error against the oracle's FP64 blend."""
+    from oracle import binding
+    mvq = max(1024, scene.num_quads)
+    rng = np.random.default_rng(seed)
+    bins = np.sort(rng.choice(r.num_bins, size=min(num_bins, r.num_bins), replace=False)).astype(np.int32)
+    img, counts, prims = r.raster_dump_bins(frame, bins, max_per_pixel)
+    o = binding.run(scene, max_visible_quads=mvq, bin_subset=bins, threads=host_cores(), image64=True,
+                    max_per_pixel=max_per_pixel, dump_by_subset=True, setup_outputs=False)
+    g = img.cpu().numpy()
+    bcx = r.bin_count_x
+    e32 = e64 = 0.0
+    for b in bins:
+        by, bx = divmod(int(b), bcx)
+        ys = slice(by * 32, min(by * 32 + 32, scene.height))
+        xs = slice(bx * 32, min(bx * 32 + 32, scene.width))
+        e32 = max(e32, float(np.abs(g[ys, xs] - o["image"][ys, xs]).max()))
+        e64 = max(e64, float(np.abs(g[ys, xs].astype(np.float64) - o["image64"][ys, xs]).max()))
+    order_ok = bool(np.array_equal(counts, o["frag_counts"]) and np.array_equal(prims, o["frag_prims"]))
+    return {"bins": int(len(bins)), "fragments": int(counts.sum()), "order_bit_exact": order_ok,
+            "max_abs_err_vs_oracle": e32, "max_abs_err_vs_fp64_blend": e64,
+            "first_fragments_compared_per_pixel": max_per_pixel}
+
+
+def workload_config(name, scene, info=None):
+    cfg = {"workload": workload_name(name), "width": scene.width, "height": scene.height,
+           "triangles": scene.num_tris}
+    if info is not None:
+        w, h = scene.width, scene.height
+        cfg.update({"fragments_per_frame": int(info.num_fragments),
+                    "blended_fragments_per_frame": int(info.raster_blended_fragments),
+                    "max_fragments_per_pixel": int(info.max_pixel_fragments),
+                    "mean_layers_per_pixel": int(info.num_fragments) / (w * h),
+                    "visible_quads": list(info.num_visible_quads),
+                    "bin_levels": {"low": info.bin_level_counts[2], "high": info.bin_level_counts[4]},
+                    "light_bins": int(info.raster_light_bins)})
+    return cfg
 
 
 def run_reference(args, rank):
-    """--impl reference: the CPU oracle (port of the reference passes) on bounded samples."""
+    """--impl reference: the CPU oracle (port of the reference passes) on all host cores, on a
+    bounded sample of the workload per step."""
     if rank != 0:
         return
     from lucid_gb300 import scenes
     scene = scenes.workload(args.workload)
     bins = args.cpu_sample_bins or 48
+    cores = host_cores()
     vals = []
     last = None
     for i in range(args.warmup + args.steps):
-        r = cpu_baseline(scene, bins, seed=i)
+        r = cpu_sample(scene, bins, cores, seed=i)
         # extrapolated whole-frame rate: total fragments / (binning + raster of all bins)
         rate = r["frag_sample"] / r["t_raster_sample"]
         frame_frags = r["frag_sample"] * r["bin_count"] / r["bins"]
@@ -196,8 +271,8 @@ def run_reference(args, rank):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": workload_name(args.workload)}, "impl": "reference",
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": last["threads"], "kind": "port",
+            "config": workload_config(args.workload, scene), "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -354,6 +429,65 @@ def quadgen_bench(steps, warmup):
             "cpu_degenerate": int(ref_nd), "cpu_cores": 1, "median_of": steps}
 
 
+def workload_bench(name, steps, warmup, flush_buf):
+    """One named workload on its own renderer: median frame time (CUDA events, L2 flushed between
+    frames), Mtri/s, fragments/s, realised depth complexity and the median time of each pass
+    (pass-level entry points, one event pair per pass)."""
+    import torch
+    from lucid_gb300 import scenes
+    from lucid_gb300.renderer import FrameInputs, LucidRenderer
+    sc = scenes.workload(name)
+    r = LucidRenderer(sc.width, sc.height, max_input_quads=sc.num_quads, max_visible_quads=sc.num_quads,
+                      max_bin_refs=8 * sc.num_quads)
+    frame = FrameInputs.from_scene(sc)
+    out = r.new_image()
+    stream = torch.cuda.current_stream()
+    for _ in range(warmup):
+        r.render(frame, out)
+    torch.cuda.synchronize()
+    passes = [("setup", lambda: r.quad_setup(frame)), ("bin_count", r.bin_count),
+              ("bin_categorize", r.bin_categorize), ("bin_dispatch", r.bin_dispatch),
+              ("raster", lambda: r.raster(frame, out))]
+    frame_ms, pass_ms = [], {n: [] for n, _ in passes}
+    for i in range(steps):
+        flush_buf.fill_(i & 0xFF)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(len(passes) + 1)]
+        ev[0].record(stream)
+        for k, (_, fn) in enumerate(passes):
+            fn()
+            ev[k + 1].record(stream)
+        torch.cuda.synchronize()
+        for k, (n, _) in enumerate(passes):
+            pass_ms[n].append(ev[k].elapsed_time(ev[k + 1]))
+        frame_ms.append(ev[0].elapsed_time(ev[-1]))
+    info, _ = r.info()
+    if info.error_code != 0:
+        raise RuntimeError(f"{name}: device error {info.error_code}")
+    t = float(np.median(frame_ms))
+    med = {n: float(np.median(v)) for n, v in pass_ms.items()}
+    frags = int(info.num_fragments)
+    res = {"config": workload_config(name, sc, info), "ms_per_frame": t,
+           "mtri_per_s": sc.num_tris / (t / 1e3) / 1e6, "fragments_per_s": frags / (t / 1e3),
+           "blended_fragments_per_s": int(info.raster_blended_fragments) / (t / 1e3),
+           "pass_ms": med, "pass_share": {n: v / sum(med.values()) for n, v in med.items()},
+           "median_of": steps}
+    r.close()
+    return res
+
+
+def profile_figures():
+    """Issue-slot figures of the raster kernel from the committed ncu summary (one launch)."""
+    path = os.path.join(ROOT, "profiles", "raster_heavy1080.md")
+    res = {}
+    if os.path.exists(path):
+        with open(path) as f:
+            for line in f:
+                for key in ("issue_active_frac", "warp_instructions_per_fragment"):
+                    if line.startswith(key + ":"):
+                        res[key] = float(line.split(":", 1)[1].split()[0])
+    return res
+
+
 def main():
     args = parse_args()
     rank, world, local = dist_setup(args.gpus)
@@ -391,6 +525,7 @@ def main():
     if info.error_code != 0:
         raise RuntimeError(f"device error {_lib.ERR_NAMES.get(info.error_code)} {tuple(info.error_detail)}")
     fragments = int(info.num_fragments)
+    blended = int(info.raster_blended_fragments)
     hblock_tris = int(info.num_hblock_tris)
     qrefs, trefs = int(info.num_bin_quad_refs), int(info.num_bin_tri_refs)
     bq = r.download(_lib.BUF_BIN_QUADS, count=qrefs)
@@ -443,10 +578,13 @@ def main():
     peak, peak_kind = measured_peaks()
     achieved = alg_bytes / (raster_ms / 1e3) / 1e9
     tpf = profile_traffic_per_fragment()
+    # frac is the HBM roofline fraction; the kernel keeps fragments on chip and is limited by
+    # issue slots and latency (issue_active_frac, warp instructions per fragment: ncu, one launch)
     roofline = {"kernel": "rasterKernel", "bound": "hbm", "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                 "traffic": None if tpf is None else tpf * fragments,
-                "algorithmic_bytes": alg_bytes, "kernel_ms": raster_ms}
+                "algorithmic_bytes": alg_bytes, "kernel_ms": raster_ms,
+                "limiter": "issue slots and latency (fragments stay in shared memory)", **profile_figures()}
 
     # ---- e2e: host buffers through lucid_render
     host = {k: getattr(frame, k).cpu().pin_memory() for k in
@@ -474,34 +612,24 @@ def main():
     fwd_bwd = grad_bench(max(5, args.steps), max(3, args.warmup), flush_buf) if extras else None
     batch = batch_bench(max(5, args.steps), max(3, args.warmup), flush_buf) if extras else None
     quadgen = quadgen_bench(max(3, min(args.steps, 5)), 1) if extras else None
+    workloads = {n: workload_bench(n, max(5, args.steps), max(3, args.warmup), flush_buf)
+                 for n in ("meshes4k", "cpu720")} if extras else None
 
-    # ---- CPU baseline (rank 0, N=1 only)
-    cpu = None
+    # ---- CPU baseline and a parity check of the benchmark frame (rank 0, N=1 only; not timed)
+    cpu = parity = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        bins = args.cpu_sample_bins or 48
-        cb = cpu_baseline(scene, bins)
-        rate = cb["frag_sample"] / cb["t_raster_sample"]
-        frame_time = cb["t_bin"] + fragments / rate
-        cpu = {"value": fragments / frame_time, "unit": UNIT, "cores": cb["threads"], "kind": "port",
-               "sample": (f"oracle setup+binning of the whole frame ({cb['t_bin']:.2f} s) and raster "
-                          f"of {cb['bins']} seeded random bins of {cb['bin_count']} "
-                          f"({cb['frag_sample']} fragments, {cb['t_raster_sample']:.2f} s); frame "
-                          f"time extrapolated to {fragments} fragments"),
-               "ms_per_frame": frame_time * 1e3}
+        cpu = cpu_baselines(scene, fragments)
+        parity = parity_sample(r, frame, scene)
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": workload_name(args.workload), "width": w, "height": h,
-                       "triangles": scene.num_tris, "fragments_per_frame": fragments,
-                       "max_fragments_per_pixel": int(info.max_pixel_fragments),
-                       "mean_layers_per_pixel": fragments / (w * h),
-                       "visible_quads": list(info.num_visible_quads),
-                       "bin_levels": {"low": info.bin_level_counts[2], "high": info.bin_level_counts[4]},
+            "config": {**workload_config(args.workload, scene, info),
                        "l2": "flushed between steps (256 MB write, outside the step events)",
                        "parallelism": f"replicas x{world}"},
+            "blended_fragments_per_s": blended * args.steps * world / (total_ms / 1e3),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms},
             "roofline": roofline,
@@ -512,6 +640,8 @@ def main():
             "fwd_bwd": fwd_bwd,
             "batch": batch,
             "quadgen": quadgen,
+            "workloads": workloads,
+            "parity": parity,
         }
         print(json.dumps(line), flush=True)
     r.close()

@@ -36,7 +36,8 @@ class Options(ctypes.Structure):
                 ("low_high_threshold", c_int32), ("max_bin_refs", c_int32),
                 ("band_capacity", c_int32), ("binning_ctas", c_int32),
                 ("raster_ctas_per_sm", c_int32), ("max_views", c_int32),
-                ("grad_store_fragments", c_int32), ("slab_fragments", c_int32), ("reserved", c_int32 * 3)]
+                ("grad_store_fragments", c_int32), ("slab_fragments", c_int32), ("light_max_pixel", c_int32),
+                ("reserved", c_int32 * 2)]
 
 
 class TextureC(ctypes.Structure):

@@ -20,6 +20,11 @@ constexpr int kMaxBinCount = 16384;      // bins of one view (128 x 128 bins = 4
 constexpr int kSetupThreads = 256;
 constexpr int kBinningThreads = 1024;
 constexpr int kRasterThreads = 512;
+// uint4 per tri of the shading record: 4 with FP16 vertex colours, 3 otherwise
+constexpr int kShadeRecWords = 4;
+__host__ __device__ __forceinline__ int shadeRecWords(int color_format) {
+	return color_format == LUCID_COLOR_RGBA16F ? 4 : 3;
+}
 
 // Per-view device parameters (passed by value to every kernel).
 struct FrameParams {
@@ -47,6 +52,7 @@ struct FrameParams {
 	int band_capacity;
 	int low_high_threshold;
 	int slab_target;      // fragments per unfinished pixel a depth slab aims at
+	int light_max_pixel;  // bins whose pixels have at most this many fragments take the light path
 	int num_setup_ctas;
 	int num_binning_ctas;
 	uint32_t flags;
@@ -67,8 +73,9 @@ struct FrameParams {
 	uint4* quad_normals;  // encoded vertex normals per quad slot (STORAGE_QUAD_NORMAL)
 	uint4* quad_tex;      // 2 per quad slot: tex0, tex1 - tex0, tex2 - tex0, tex3 - tex0
 	uint4* tri_bary;  // 2 per tri
-	uint4* tri_shade; // 3 per tri: the two tri_bary records, then the tri's RGBA8 vertex colours
-	                  // (when the instance has them) and its instance flags | id << 16
+	uint4* tri_shade; // shadeRecWords(color_format) per tri: the two tri_bary records, then the vertex
+	                  // colours (RGBA8 or FP16, when the instance has them) and its instance
+	                  // flags | id << 16 (ShadeRec in lucid_shade.cuh)
 	uint4* tri_scan;  // 2 per tri
 	uint4* tri_depth; // 1 per tri
 	uint32_t* tri_normals;

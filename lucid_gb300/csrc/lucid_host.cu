@@ -186,6 +186,10 @@ void setShadingInputs(FrameParams& p, const lucid_frame_inputs* in) {
 
 // fragments per unfinished pixel that a depth slab of the raster aims at
 int slabTarget(const lucid_renderer* r) { return r->opts.slab_fragments > 0 ? r->opts.slab_fragments : 180; }
+// deepest pixel of a bin that takes the light raster path (-1: none)
+int lightMaxPixel(const lucid_renderer* r) {
+	return r->opts.light_max_pixel == 0 ? 64 : (r->opts.light_max_pixel < 0 ? -1 : r->opts.light_max_pixel);
+}
 
 FrameParams makeParams(lucid_renderer* r, const lucid_frame_inputs* in, float* out) {
 	FrameParams p{};
@@ -209,6 +213,7 @@ FrameParams makeParams(lucid_renderer* r, const lucid_frame_inputs* in, float* o
 	p.band_capacity = r->opts.band_capacity;
 	p.low_high_threshold = r->opts.low_high_threshold;
 	p.slab_target = slabTarget(r);
+	p.light_max_pixel = lightMaxPixel(r);
 	p.num_setup_ctas = (in->num_quads + kSetupThreads - 1) / kSetupThreads;
 	p.num_binning_ctas = r->opts.binning_ctas;
 	p.flags = r->opts.flags;
@@ -464,7 +469,7 @@ extern "C" lucid_status lucid_create(const lucid_options* options, int32_t width
 	   (st = allocate(r, &r->quad_normals, mvq)) != LUCID_OK ||
 	   (st = allocate(r, &r->quad_tex, 2 * mvq)) != LUCID_OK ||
 	   (st = allocate(r, &r->tri_bary, 4 * mvq)) != LUCID_OK ||
-	   (st = allocate(r, &r->tri_shade, 6 * mvq)) != LUCID_OK ||
+	   (st = allocate(r, &r->tri_shade, 2 * kShadeRecWords * mvq)) != LUCID_OK ||
 	   (st = allocate(r, &r->tri_scan, 4 * mvq)) != LUCID_OK ||
 	   (st = allocate(r, &r->tri_depth, 2 * mvq)) != LUCID_OK ||
 	   (st = allocate(r, &r->tri_normals, 2 * mvq)) != LUCID_OK ||
@@ -606,6 +611,7 @@ static lucid_status rasterImpl(lucid_renderer* r, const lucid_frame_inputs* in, 
 	r->grad_ready = false;
 	FrameParams p = r->last;
 	p.slab_target = slabTarget(r);
+	p.light_max_pixel = lightMaxPixel(r);
 	p.colors = in->colors;
 	p.color_format = in->color_format;
 	p.instance_colors = in->instance_colors;
@@ -1085,6 +1091,7 @@ void batchParams(lucid_renderer* r, BatchPlan* b, const lucid_view* views, std::
 		p.band_capacity = r->opts.band_capacity;
 		p.low_high_threshold = r->opts.low_high_threshold;
 		p.slab_target = slabTarget(r);
+		p.light_max_pixel = lightMaxPixel(r);
 		p.num_setup_ctas = viewSetupCtas(nq);
 		p.num_binning_ctas = b->binning_ctas[size_t(v)];
 		p.flags = r->opts.flags & ~uint32_t(LUCID_OPT_TIMERS);
@@ -1101,7 +1108,7 @@ void batchParams(lucid_renderer* r, BatchPlan* b, const lucid_view* views, std::
 		p.quad_normals = r->quad_normals + qbase;
 		p.quad_tex = r->quad_tex + 2 * qbase;
 		p.tri_bary = r->tri_bary + 4 * qbase;
-		p.tri_shade = r->tri_shade + 6 * qbase;
+		p.tri_shade = r->tri_shade + 2 * kShadeRecWords * qbase;
 		p.tri_scan = r->tri_scan + 4 * qbase;
 		p.tri_depth = r->tri_depth + 2 * qbase;
 		p.tri_normals = r->tri_normals + 2 * qbase;

@@ -54,8 +54,8 @@ constexpr int kHistWords = 8192;    // per-group depth histogram (pixels x bucke
 constexpr int kCoarseShift = 20;    // fragment estimate bins: depth keys >> 20 (4096 bins)
 constexpr int kCoarseBins = 1 << (32 - kCoarseShift);
 constexpr int kMaxSlabs = 64;       // depth slabs of one group at most
-// light bins: at most kLightPixel fragments per pixel, so one row's fragments fit a warp's
-// kLightPool-entry slice of the sort buffers
+// light bins: each pass of a row keeps at most kLightPixel fragments per pixel, so they fit a
+// warp's kLightPool-entry slice of the sort buffers
 constexpr int kLightPixel = 32;
 constexpr int kLightPool = 32 * kLightPixel;
 
@@ -454,28 +454,81 @@ __device__ __forceinline__ uint32_t triPrim(const FrameParams& p, uint32_t tri) 
 	return __ldg(p.quad_source + (tri >> 1)) * 2 + (tri & 1);
 }
 
-// One row of a light bin, by one warp (lane = pixel column): every fragment of the row goes
-// into the warp's pool (K: depth keys, V: tri slots), the lane's pixel at [off, off + count);
-// then each lane blends its pixel front to back, taking the nearest remaining fragment (ties by
-// input primitive id) each step, and stops once T == 0: nothing behind that point is ordered or
-// shaded. The keys, shading and blend are the FP32 expressions of the group path
+// (key, prim) order of two fragments of one pixel: nearest first, equal keys by input primitive
+// id (looked up only for equal keys; a tri covers a pixel once, so the order is strict).
+__device__ __forceinline__ bool fragBefore(const FrameParams& p, uint32_t ka, uint32_t ta, uint32_t kb, uint32_t tb) {
+	return ka < kb || (ka == kb && triPrim(p, ta) < triPrim(p, tb));
+}
+
+// One row of a light bin, by one warp (lane = pixel column). In each pass every lane gathers,
+// from the band entries of the row, the nearest min(count, kLightPixel) fragments of its pixel
+// behind the last fragment it has blended (all of them when the pixel has no more) into its
+// slots of the warp's pool (K: depth keys, V: tri slots), then blends them front to back,
+// taking the nearest remaining one each step, and stops once T == 0: nothing behind that point
+// is ordered or shaded. A pixel with more fragments than slots whose T is still above 0 takes
+// another pass. Keys, shading and blend are the FP32 expressions of the group path
 // (shading.glsl:116, :279-280, :312). Returns the fragments the lane blended.
+// A row whose pixels all fit their slots (the common case) is gathered with lane = band entry
+// instead: each lane walks its entry's span in the row and appends the fragments to their
+// pixels through per-pixel cursors (`cursor`, 32 ints of the warp), so that every lane does
+// useful work; the order inside a pixel's slots does not matter, the blend selects by
+// (key, prim).
 __device__ unsigned long long lightRow(const FrameParams& p, const RasterSmem& s, const uint2* scratch,
 									   const float4* planes, int band_cap, int bin, int bin_x, int bin_y, int row,
-									   uint32_t* K, uint32_t* V, float4 bg, bool additive, bool alpha_threshold,
-									   bool dump) {
+									   uint32_t* K, uint32_t* V, int* cursor, float4 bg, bool additive,
+									   bool alpha_threshold, bool dump, long long* tacc) {
 	const int lane = threadIdx.x & 31;
+	long long t0 = tacc ? clock64() : 0;
 	const int pl = row * 32 + lane;
 	const int cnt = s.pix_count[pl];
-	const int off = warpInclusiveScan(cnt) - cnt;
+	const int cap = min(cnt, kLightPixel);
+	const int off = warpInclusiveScan(cap) - cap;
 	const int px = bin_x + lane, py = bin_y + row;
-	// A. the row's fragments from the band entries (spans already clipped to the viewport)
-	int cur = off;
-	const int end = off + cnt;
-	if(__any_sync(0xffffffffu, cnt > 0)) {
-		const int b = row >> 2, rshift = 5 * (row & 3);
-		const int ne = s.band_count[b];
-		const float fx = float(px), fy = float(py);
+	const float fx = float(px), fy = float(py);
+	const int b = row >> 2, rshift = 5 * (row & 3);
+	const int ne = s.band_count[b];
+	float T = 1.0f, c0 = 0.0f, c1 = 0.0f, c2 = 0.0f;
+	int k = 0, remaining = cnt;
+	bool have_thr = false; // the last blended fragment: later passes gather what lies behind it
+	uint32_t thr_key = 0u, thr_tri = 0u;
+	bool done = cnt == 0;
+	const long long dbase = dump ? dumpPixel(p, bin, pl, px, py) : -1;
+	int row_max = cnt;
+#pragma unroll
+	for(int o = 16; o > 0; o >>= 1)
+		row_max = max(row_max, __shfl_xor_sync(0xffffffffu, row_max, o));
+	bool single = row_max <= kLightPixel; // one pass gathers every fragment of the row
+	while(__any_sync(0xffffffffu, !done)) {
+		// A. the pass's fragments from the band entries (spans already clipped to the viewport)
+		const bool want = !done;
+		const bool bounded = remaining > cap; // keep only the nearest `cap`
+		int size = 0, maxi = 0;
+		uint32_t maxk = 0u, maxt = 0u;
+		if(single) {
+			cursor[lane] = off;
+			__syncwarp();
+			for(int j = lane; j < ne; j += 32) {
+				const uint2 e = scratch[size_t(b) * band_cap + j];
+				const int lo = (e.x >> rshift) & 31, hi = (e.y >> rshift) & 31;
+				if(lo > hi)
+					continue;
+				const float4 d = planes[size_t(b) * band_cap + j];
+				const uint32_t t = entryTri(e);
+				const float ty = d.y * fy + d.z;
+				for(int x = lo; x <= hi; x++) {
+					const uint32_t key = nearFirstKey(d.x * float(bin_x + x) + ty);
+					const int pos = atomicAdd(&cursor[x], 1);
+					if(pos < kLightPool) {
+						K[pos] = key;
+						V[pos] = t;
+					}
+				}
+			}
+			__syncwarp();
+			size = cursor[lane] - off;
+			__syncwarp();
+			single = false;
+		} else
 		for(int j0 = 0; j0 < ne; j0 += 32) {
 			const int j = j0 + lane;
 			bool rel = j < ne;
@@ -495,12 +548,12 @@ __device__ unsigned long long lightRow(const FrameParams& p, const RasterSmem& s
 			}
 			uint32_t todo = __ballot_sync(0xffffffffu, rel);
 			while(todo != 0u) {
-				int k[4];
+				int kk[4];
 				bool has[4];
 #pragma unroll
 				for(int u = 0; u < 4; u++) {
 					has[u] = todo != 0u;
-					k[u] = has[u] ? __ffs(todo) - 1 : 0;
+					kk[u] = has[u] ? __ffs(todo) - 1 : 0;
 					if(has[u])
 						todo &= todo - 1u;
 				}
@@ -508,60 +561,107 @@ __device__ unsigned long long lightRow(const FrameParams& p, const RasterSmem& s
 				float kdx[4], kty[4];
 #pragma unroll
 				for(int u = 0; u < 4; u++) {
-					sp[u] = __shfl_sync(0xffffffffu, span, k[u]);
-					kdx[u] = __shfl_sync(0xffffffffu, dx, k[u]);
-					kty[u] = __shfl_sync(0xffffffffu, ty, k[u]);
-					tr[u] = __shfl_sync(0xffffffffu, tri, k[u]);
+					sp[u] = __shfl_sync(0xffffffffu, span, kk[u]);
+					kdx[u] = __shfl_sync(0xffffffffu, dx, kk[u]);
+					kty[u] = __shfl_sync(0xffffffffu, ty, kk[u]);
+					tr[u] = __shfl_sync(0xffffffffu, tri, kk[u]);
 				}
 #pragma unroll
-				for(int u = 0; u < 4; u++)
-					if(has[u] && lane >= int(sp[u] & 31u) && lane <= int(sp[u] >> 5)) {
-						if(cur < end) {
-							K[cur] = nearFirstKey(kdx[u] * fx + kty[u]);
-							V[cur] = tr[u];
-						}
-						cur++;
+				for(int u = 0; u < 4; u++) {
+					if(!(want && has[u] && lane >= int(sp[u] & 31u) && lane <= int(sp[u] >> 5)))
+						continue;
+					const uint32_t key = nearFirstKey(kdx[u] * fx + kty[u]), t = tr[u];
+					if(have_thr && !fragBefore(p, thr_key, thr_tri, key, t))
+						continue; // blended in an earlier pass
+					if(size < cap) {
+						K[off + size] = key;
+						V[off + size] = t;
+						if(bounded && (size == 0 || fragBefore(p, maxk, maxt, key, t)))
+							maxk = key, maxt = t, maxi = size;
+						size++;
+					} else if(fragBefore(p, key, t, maxk, maxt)) {
+						// full: the new fragment replaces the farthest one kept
+						K[off + maxi] = key;
+						V[off + maxi] = t;
+						maxi = 0, maxk = K[off], maxt = V[off];
+						for(int i = 1; i < cap; i++)
+							if(fragBefore(p, maxk, maxt, K[off + i], V[off + i]))
+								maxi = i, maxk = K[off + i], maxt = V[off + i];
 					}
+				}
 			}
 		}
-	}
-	__syncwarp();
-	if(cur != end)
-		raiseError(p.info, LUCID_ERR_BIN_COUNT, uint32_t(bin), uint32_t(pl), uint32_t(cur - off));
-	// B. front-to-back blend by selection
-	float T = 1.0f, c0 = 0.0f, c1 = 0.0f, c2 = 0.0f;
-	int n = min(cur, end) - off, k = 0;
-	long long dbase = dump ? dumpPixel(p, bin, pl, px, py) : -1;
-	while(n > 0) {
-		if(!additive && !dump && T == 0.0f)
-			break;
-		int bi = off;
-		uint32_t bk = K[off];
-		for(int i = off + 1; i < off + n; i++) {
-			const uint32_t ki = K[i];
-			if(ki < bk || (ki == bk && triPrim(p, V[i]) < triPrim(p, V[bi])))
-				bi = i, bk = ki;
+		__syncwarp();
+		if(tacc && lane == 0) {
+			const long long t1 = clock64();
+			tacc[3] += t1 - t0;
+			t0 = t1;
 		}
-		const uint32_t tri = V[bi];
-		K[bi] = K[off + n - 1];
-		V[bi] = V[off + n - 1];
-		n--;
-		const float4 c = shadeFragment(p, tri, keyToDepth(bk), px, py);
-		if(dbase >= 0 && k < p.dump_max)
-			p.dump_prims[size_t(dbase) * p.dump_max + k] = int(triPrim(p, tri));
-		k++;
-		const float qx = c.x * c.w, qy = c.y * c.w, qz = c.z * c.w;
-		if(additive) {
-			c0 = c0 + qx;
-			c1 = c1 + qy;
-			c2 = c2 + qz;
-		} else {
-			c0 = c0 + qx * T;
-			c1 = c1 + qy * T;
-			c2 = c2 + qz * T;
-			T = T * (1.0f - c.w);
-			if(alpha_threshold && T < (1.0f / 128.0f))
-				break;
+		if(want && size != min(remaining, cap)) {
+			raiseError(p.info, LUCID_ERR_BIN_COUNT, uint32_t(bin), uint32_t(pl), uint32_t(size));
+			done = true;
+		}
+		// B. front-to-back blend by selection; the next fragment's shading record is loaded while
+		// the current one is shaded
+		int n = want && !done ? size : 0;
+		auto take = [&](uint32_t& key, uint32_t& tri) {
+			int bi = off;
+			key = K[off];
+			for(int i = off + 1; i < off + n; i++) {
+				const uint32_t ki = K[i];
+				if(ki < key || (ki == key && triPrim(p, V[i]) < triPrim(p, V[bi])))
+					bi = i, key = ki;
+			}
+			tri = V[bi];
+			K[bi] = K[off + n - 1];
+			V[bi] = V[off + n - 1];
+			n--;
+		};
+		bool stop = false;
+		if(n > 0) {
+			uint32_t ck, ct;
+			take(ck, ct);
+			ShadeRec cr = loadShadeRec(p, ct);
+			while(true) {
+				uint32_t nk = 0u, nt = 0u;
+				ShadeRec nr;
+				const bool more = n > 0;
+				if(more) {
+					take(nk, nt);
+					nr = loadShadeRec(p, nt);
+				}
+				const float4 c = shadeCoreRec(p, ct, cr, keyToDepth(ck), px, py).col;
+				if(dbase >= 0 && k < p.dump_max)
+					p.dump_prims[size_t(dbase) * p.dump_max + k] = int(triPrim(p, ct));
+				k++;
+				remaining--;
+				have_thr = true, thr_key = ck, thr_tri = ct;
+				const float qx = c.x * c.w, qy = c.y * c.w, qz = c.z * c.w;
+				if(additive) {
+					c0 = c0 + qx;
+					c1 = c1 + qy;
+					c2 = c2 + qz;
+				} else {
+					c0 = c0 + qx * T;
+					c1 = c1 + qy * T;
+					c2 = c2 + qz * T;
+					T = T * (1.0f - c.w);
+					if((T == 0.0f && !dump) || (alpha_threshold && T < (1.0f / 128.0f))) {
+						stop = true;
+						break;
+					}
+				}
+				if(!more)
+					break;
+				ck = nk, ct = nt, cr = nr;
+			}
+		}
+		if(want)
+			done = done || stop || remaining == 0;
+		if(tacc && lane == 0) {
+			const long long t1 = clock64();
+			tacc[5] += t1 - t0;
+			t0 = t1;
 		}
 	}
 	float4 o;
@@ -670,7 +770,8 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 	// Section timers (timers.glsl:9-39): thread 0 accumulates clock64 deltas between the
 	// CTA-wide barriers that separate the phases; units of 256 cycles in lucid_info.raster_timers:
 	// 0 row spans, 1 counts, 2 depth histograms, 3 window fragments, 4 sort, 5 shading,
-	// 6 blending, 7 output and bin fetch.
+	// 6 blending, 7 output and bin fetch. Light bins: 3 fragments and 5 blend of warp 0's rows,
+	// 6 the wait for the other warps.
 	lucid_info* const timer_info = work.timerInfo();
 	const bool timers = (opt_flags & LUCID_OPT_TIMERS) != 0 && timer_info != nullptr;
 	long long tacc[8] = {0, 0, 0, 0, 0, 0, 0, 0}, tlast = timers ? clock64() : 0;
@@ -861,13 +962,19 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 		// ---- L. light bins (every pixel has at most kLightPixel fragments): one warp per row,
 		// no CTA barrier until the bin is done
 		if constexpr(MODE == kRasterForward) {
-			if(s.bin_maxpx <= kLightPixel) {
+			if(s.bin_maxpx <= p.light_max_pixel) {
 				uint32_t* K = &s.kv[0][0][0] + warp * kLightPool;
 				uint32_t* V = &s.kv[0][0][0] + NW * kLightPool + warp * kLightPool;
 				unsigned long long blended = 0;
+				// timers: warp 0's rows split into generation (3) and blend (5); the wait for the
+				// other warps at the end of the bin goes to 6
+				long long* ta = timers && tid == 0 ? tacc : nullptr;
+				int* cursor = &s.eff_prefix[warp * 32];
 				for(int row = warp; row < 32; row += NW)
-					blended += lightRow(p, s, scratch, planes, band_cap, bin, bin_x, bin_y, row, K, V, bg, additive,
-										alpha_threshold, dump);
+					blended += lightRow(p, s, scratch, planes, band_cap, bin, bin_x, bin_y, row, K, V, cursor, bg,
+										additive, alpha_threshold, dump, ta);
+				if(ta)
+					tlast = clock64();
 #pragma unroll
 				for(int o = 16; o > 0; o >>= 1)
 					blended += __shfl_xor_sync(0xffffffffu, blended, o);
@@ -876,7 +983,7 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 				if(tid == 0)
 					atomicAdd(&p.info->raster_light_bins, 1u);
 				__syncthreads();
-				RASTER_TIMER(3);
+				RASTER_TIMER(6);
 				continue;
 			}
 		}
@@ -1520,8 +1627,10 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 							// pixel's cursor is not read again.
 							const float4* sp = stage + t * batch;
 							const int n = min(batch, fend - f);
+							int on_steps = 0; // fragments blended (before T reached 0)
 							auto step = [&](float4 q) {
 								const bool on = T != 0.0f;
+								on_steps += on ? 1 : 0;
 								c0 = c0 + (on ? q.x * T : -0.0f);
 								c1 = c1 + (on ? q.y * T : -0.0f);
 								c2 = c2 + (on ? q.z * T : -0.0f);
@@ -1542,6 +1651,8 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 							for(; T != 0.0f && j < n; j++)
 								step(sp[j]);
 							finished = T == 0.0f;
+							if constexpr(MODE == kRasterForward)
+								nblend += (unsigned long long)on_steps - (unsigned long long)j; // j is added below
 							f += j;
 						} else
 						for(int j = 0; j < batch && f < fend; j++, f++) {

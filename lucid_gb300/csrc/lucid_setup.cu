@@ -208,7 +208,7 @@ __device__ __forceinline__ QuadClass processInputQuad(const FrameParams& p, cons
 // storeTri (quad_setup.glsl:274-340)
 __device__ __forceinline__ void storeTri(const FrameParams& p, const lucid_config& cfg, F3 ray_dir0,
 						 uint32_t tri_idx, uint32_t inst_flags_id, F3 tri0, F3 tri1, F3 tri2,
-						 uint32_t y_aabb, uint3 colors) {
+						 uint32_t y_aabb, uint3 colors, const uint2* half_colors) {
 	F3 dirx = xyz4(cfg.frustum.ws_dirx), diry = xyz4(cfg.frustum.ws_diry);
 	F3 dir0 = xyz4(cfg.frustum.ws_dir0);
 	F3 normal = cross3(tri0 - tri2, tri1 - tri0);
@@ -237,10 +237,17 @@ __device__ __forceinline__ void storeTri(const FrameParams& p, const lucid_confi
 	const uint4 bary1 = make_uint4(fbits(e1.x), fbits(e1.y), fbits(e1.z), fbits(param1));
 	p.tri_bary[size_t(tri_idx) * 2 + 0] = bary0;
 	p.tri_bary[size_t(tri_idx) * 2 + 1] = bary1;
-	// the shading record: what a fragment of the tri reads, in 48 contiguous bytes
-	p.tri_shade[size_t(tri_idx) * 3 + 0] = bary0;
-	p.tri_shade[size_t(tri_idx) * 3 + 1] = bary1;
-	p.tri_shade[size_t(tri_idx) * 3 + 2] = make_uint4(colors.x, colors.y, colors.z, inst_flags_id);
+	// the shading record: what a fragment of the tri reads, in 48 (64 with FP16 colours)
+	// contiguous bytes (layout: ShadeRec in lucid_shade.cuh)
+	uint4* rec = p.tri_shade + size_t(tri_idx) * shadeRecWords(p.color_format);
+	rec[0] = bary0;
+	rec[1] = bary1;
+	if(half_colors) {
+		rec[2] = make_uint4(half_colors[0].x, half_colors[0].y, half_colors[1].x, inst_flags_id);
+		rec[3] = make_uint4(half_colors[1].y, half_colors[2].x, half_colors[2].y, 0u);
+	} else {
+		rec[2] = make_uint4(colors.x, colors.y, colors.z, inst_flags_id);
+	}
 
 	F3 nrm0 = cross3(tri2, tri1 - tri2);
 	F3 nrm1 = cross3(tri0, tri2 - tri0);
@@ -429,6 +436,14 @@ template <class Src> __global__ void __launch_bounds__(kSetupThreads) setupStore
 		qc = make_uint4(__ldg(cols + v[0]), __ldg(cols + v[1]), __ldg(cols + v[2]), __ldg(cols + v[3]));
 		p.quad_colors[slot] = qc;
 	}
+	uint2 hq[4]; // FP16 vertex colours of the quad (into the tris' shading records)
+	const bool half_vc = (flags & LUCID_INST_HAS_VERTEX_COLORS) && p.color_format == LUCID_COLOR_RGBA16F;
+	if(half_vc) {
+		const uint2* hc = reinterpret_cast<const uint2*>(p.colors);
+#pragma unroll
+		for(int i = 0; i < 4; i++)
+			hq[i] = __ldg(hc + v[i]);
+	}
 	// storeQuad (quad_setup.glsl:256-272): vertex normals, texture coordinates relative to the
 	// first vertex
 	if((flags & LUCID_INST_HAS_VERTEX_NORMALS) && p.normals)
@@ -454,8 +469,10 @@ template <class Src> __global__ void __launch_bounds__(kSetupThreads) setupStore
 		F3 t0 = loadVertex(p.positions, v[0]) - origin;
 		F3 t1 = loadVertex(p.positions, v[1 + second]) - origin;
 		F3 t2 = loadVertex(p.positions, v[2 + second]) - origin;
+		const uint2 ht[3] = {hq[0], second ? hq[2] : hq[1], second ? hq[3] : hq[2]};
 		storeTri(p, cfg, ray_dir0, uint32_t(slot) * 2 + second, inst_flags_id, t0, t1, t2,
-				 second ? rec.z : rec.y, make_uint3(qc.x, second ? qc.z : qc.y, second ? qc.w : qc.z));
+				 second ? rec.z : rec.y, make_uint3(qc.x, second ? qc.z : qc.y, second ? qc.w : qc.z),
+				 half_vc ? ht : nullptr);
 	}
 }
 

@@ -116,11 +116,34 @@ struct ShadeCore {
 	uint32_t prim;
 };
 
-__device__ __forceinline__ ShadeCore shadeCore(const FrameParams& p, uint32_t tri, float inv_ray_pos, int px, int py) {
+// A tri's shading record (shadeRecWords(color_format) uint4 per tri, written by setup): the two barycentric
+// plane records, then the vertex colours and instance flags | id << 16 (in c.w):
+//   RGBA8:   c = (c0, c1, c2, flags_id)
+//   RGBA16F: c = (c0.rg, c0.ba, c1.rg, flags_id), c2 = (c1.ba, c2.rg, c2.ba, 0) (IEEE halves)
+//   RGBA32F: c = (0, 0, 0, flags_id); the colours are read from the inputs by vertex id
+struct ShadeRec {
+	uint4 b0, b1, c, c2;
+};
+
+__device__ __forceinline__ ShadeRec loadShadeRec(const FrameParams& p, uint32_t tri) {
+	const bool half = p.color_format == LUCID_COLOR_RGBA16F;
+	const uint4* rec = p.tri_shade + size_t(tri) * (half ? 4 : 3);
+	ShadeRec r;
+	r.b0 = __ldg(rec), r.b1 = __ldg(rec + 1), r.c = __ldg(rec + 2);
+	r.c2 = half ? __ldg(rec + 3) : make_uint4(0u, 0u, 0u, 0u);
+	return r;
+}
+
+__device__ __forceinline__ float4 halfRGBA(uint32_t rg, uint32_t ba) {
+	__half2 a = *reinterpret_cast<__half2*>(&rg), b = *reinterpret_cast<__half2*>(&ba);
+	float2 fa = __half22float2(a), fb = __half22float2(b);
+	return make_float4(fa.x, fa.y, fb.x, fb.y);
+}
+
+__device__ __forceinline__ ShadeCore shadeCoreRec(const FrameParams& p, uint32_t tri, const ShadeRec& r,
+												   float inv_ray_pos, int px, int py) {
 	ShadeCore s;
-	// the tri's shading record: barycentric planes, RGBA8 vertex colours, instance flags and id
-	const uint4* rec = p.tri_shade + size_t(tri) * 3;
-	const uint4 b0r = __ldg(rec), b1r = __ldg(rec + 1), crec = __ldg(rec + 2);
+	const uint4 b0r = r.b0, b1r = r.b1, crec = r.c;
 	const uint32_t fid = crec.w;
 	const float fx = float(px), fy = float(py);
 	const float ray_pos = 1.0f / inv_ray_pos;
@@ -167,25 +190,20 @@ __device__ __forceinline__ ShadeCore shadeCore(const FrameParams& p, uint32_t tr
 	s.factor = col;
 	const float w = (1.0f - b0) - b1;
 	s.wgt = w;
-	s.vid[0] = s.vid[1] = s.vid[2] = 0u; // only read with vertex colours
+	s.vid[0] = s.vid[1] = s.vid[2] = 0u; // only read with FP32 vertex colours (gradients)
 	if(s.flags & LUCID_INST_HAS_VERTEX_COLORS) {
-		const uint4 qv = __ldg(p.quad_verts + quad);
-		s.vid[0] = qv.x, s.vid[1] = second ? qv.z : qv.y, s.vid[2] = second ? qv.w : qv.z;
 		float4 c0, c1, c2;
 		if(p.color_format == LUCID_COLOR_RGBA8) {
 			c0 = decodeRGBA8(crec.x);
 			c1 = decodeRGBA8(crec.y);
 			c2 = decodeRGBA8(crec.z);
 		} else if(p.color_format == LUCID_COLOR_RGBA16F) {
-			const uint2* hc = reinterpret_cast<const uint2*>(p.colors);
-			const uint2 h0 = __ldg(hc + s.vid[0]), h1 = __ldg(hc + s.vid[1]), h2 = __ldg(hc + s.vid[2]);
-			auto cvt = [](uint2 h) {
-				__half2 a = *reinterpret_cast<__half2*>(&h.x), b = *reinterpret_cast<__half2*>(&h.y);
-				float2 fa = __half22float2(a), fb = __half22float2(b);
-				return make_float4(fa.x, fa.y, fb.x, fb.y);
-			};
-			c0 = cvt(h0), c1 = cvt(h1), c2 = cvt(h2);
+			c0 = halfRGBA(crec.x, crec.y);
+			c1 = halfRGBA(crec.z, r.c2.x);
+			c2 = halfRGBA(r.c2.y, r.c2.z);
 		} else {
+			const uint4 qv = __ldg(p.quad_verts + quad);
+			s.vid[0] = qv.x, s.vid[1] = second ? qv.z : qv.y, s.vid[2] = second ? qv.w : qv.z;
 			const float4* fc = reinterpret_cast<const float4*>(p.colors);
 			c0 = __ldg(fc + s.vid[0]), c1 = __ldg(fc + s.vid[1]), c2 = __ldg(fc + s.vid[2]);
 		}
@@ -204,6 +222,10 @@ __device__ __forceinline__ ShadeCore shadeCore(const FrameParams& p, uint32_t tr
 	}
 	s.col = col;
 	return s;
+}
+
+__device__ __forceinline__ ShadeCore shadeCore(const FrameParams& p, uint32_t tri, float inv_ray_pos, int px, int py) {
+	return shadeCoreRec(p, tri, loadShadeRec(p, tri), inv_ray_pos, px, py);
 }
 
 // Fragment colour of the exact mode (shading.glsl:107-165 without lighting; FP32 colours).

@@ -118,14 +118,16 @@ class LucidRenderer:
     * grad_store_fragments: fragment store of the differentiable frame (0 grows on demand, < 0
       none);
     * slab_fragments: fragments per unfinished pixel that a depth slab of the raster's per-pixel
-      histograms aims at (0 = 180).
+      histograms aims at (0 = 180);
+    * light_max_pixel: bins whose pixels have at most this many fragments take the light raster
+      path (0 = 64, < 0 = off).
     """
 
     def __init__(self, width: int, height: int, *, max_input_quads: int | None = None,
                  max_visible_quads: int | None = None, max_bin_refs: int | None = None,
                  band_capacity: int | None = None, flags: int = 0, low_high_threshold: int = 1024,
                  raster_ctas_per_sm: int = 0, binning_ctas: int = 0, max_views: int = 1,
-                 grad_store_fragments: int = 0, slab_fragments: int = 0):
+                 grad_store_fragments: int = 0, slab_fragments: int = 0, light_max_pixel: int = 0):
         if not torch.cuda.is_available():
             raise RuntimeError("lucid_gb300 needs a CUDA device")
         self.lib = _lib.load()
@@ -145,6 +147,7 @@ class LucidRenderer:
         o.max_views = int(max_views)
         o.grad_store_fragments = int(grad_store_fragments)
         o.slab_fragments = int(slab_fragments)
+        o.light_max_pixel = int(light_max_pixel)
         self.options = o
         self.width, self.height = int(width), int(height)
         self.bin_count_x = (self.width + 31) // 32

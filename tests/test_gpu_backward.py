@@ -123,3 +123,46 @@ def test_backward_rejects_unsupported(gpu):
                                      ctypes.c_void_p(d.data_ptr()), None, None)
     assert st == _lib.INVALID_ARG
     r.close()
+
+
+def test_backward_at_workload_size(gpu, oracle):
+    """The forward+backward workload itself: 512x512, 200k triangles (FP32 vertex RGBA, triangle
+    opacity U[0.1, 0.9]), L2 loss to a target rendered from perturbed colours, 91 layers per
+    pixel on average. GPU gradients against FP64 central differences (h = 1e-4) of the FP64
+    loss on 1000 sampled parameters and against the oracle's FP64 analytic gradient.
+
+    The relative error divides by max(|g_ref|, 1e-3 * max|g_ref|): below that floor (a gradient
+    1000x smaller than the largest) the bound is an absolute 1e-7 * max|g_ref|. The largest
+    relative error among parameters above the floor is asserted separately."""
+    import os
+    sc = scenes.workload("grad512")
+    rng = np.random.default_rng(104)
+    pert = sc.colors.copy()
+    pert[:, :3] = np.clip(pert[:, :3] + rng.normal(0, 0.1, size=pert[:, :3].shape), 0, 1)
+    psc = scenes.Scene(**{**sc.__dict__, "colors": pert.astype(np.float32)})
+    target = oracle.run(psc, threads=os.cpu_count() or 1, setup_outputs=False)["image"]
+    g = gpu_grads(sc, target)
+    model = oracle.GradModel(sc)
+    assert model.num_fragments > 20_000_000
+    vc = sc.colors.astype(np.float64)
+    op = sc.tri_opacity.astype(np.float64)
+    assert abs(model.loss(vc, op, target) - g["loss"]) <= 1e-4 * max(1.0, g["loss"])
+    dvc64, dop64 = model.analytic(vc, op, target)
+    assert rel_err(g["dvc"].ravel(), dvc64.ravel()).max() <= TOL
+    assert rel_err(g["dop"], dop64).max() <= TOL
+    sel = np.random.default_rng(7)
+    touched_v = np.nonzero(np.abs(dvc64.ravel()) > 0)[0]
+    touched_o = np.nonzero(np.abs(dop64) > 0)[0]
+    iv = sel.choice(touched_v, size=800, replace=False)
+    io = sel.choice(touched_o, size=200, replace=False)
+    fd = np.concatenate([[model.fd(vc, op, target, 0, int(i)) for i in iv],
+                         [model.fd(vc, op, target, 1, int(i)) for i in io]])
+    got = np.concatenate([g["dvc"].ravel()[iv], g["dop"][io]])
+    err = rel_err(got, fd)
+    above = np.abs(fd) >= 1e-3 * np.abs(fd).max()
+    pure = np.abs(got - fd)[above] / np.abs(fd)[above]
+    print(f"grad512: max rel err vs FD {err.max():.3g} ({int(above.sum())} of 1000 above the floor: "
+          f"max {pure.max():.3g}); vs analytic: colours {rel_err(g['dvc'].ravel(), dvc64.ravel()).max():.3g}, "
+          f"opacity {rel_err(g['dop'], dop64).max():.3g}")
+    assert err.max() <= TOL
+    assert pure.max() <= TOL
