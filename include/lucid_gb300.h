@@ -208,6 +208,12 @@ typedef struct lucid_info {
                                            * window, lit sRGB RGBA8 shading (raster_low/high.glsl,
                                            * shading.glsl); not with ALPHA_THRESHOLD, gradients or
                                            * batches */
+#define LUCID_OPT_SORTED_BIN_LISTS 0x40u  /* binning: sort every bin's quad and tri reference
+                                           * lists by slot after the dispatcher, so that the
+                                           * lists are reproducible bit for bit (the order
+                                           * inside a bin otherwise follows the dispatcher's
+                                           * atomics, as in the reference; the image does not
+                                           * depend on it) */
 #define LUCID_OPT_PIXEL_BLEND 0x10u       /* raster pass stores each pixel's sorted fragment
                                            * list; a pixel-parallel kernel shades and blends it
                                            * (same image bits; lucid_autotune picks it per scene) */
@@ -439,16 +445,19 @@ typedef struct lucid_tuning {
 	int32_t num_candidates;     /* configurations timed                                         */
 	float frame_ms;             /* median frame time of the winner                               */
 	float default_ms;           /* median frame time of the renderer's options before tuning     */
-	int32_t reserved[2];
+	int32_t light_max_pixel;    /* deepest pixel of a bin rastered one warp per row (-1: none)  */
+	int32_t reserved[1];
 } lucid_tuning;
 
 /* Autotuner (no reference counterpart): times lucid_render of `inputs` into scratch_rgba
  * (device, width*height*4 floats) under candidate configurations, by coordinate descent over
  * the blend strategy (raster-pass blend or LUCID_OPT_PIXEL_BLEND), the LOW/HIGH threshold
- * (256, 1024, 4096) and the binning CTAs (1 or 2 per SM, within options.binning_ctas); CUDA
- * events on `stream`, median of 3 frames after one warm-up frame each. The winner is stored in
- * the renderer's options and returned in *out (may be NULL). Synchronous. Bin size is fixed at
- * 32 (the reference's only size); raster CTAs are one per SM (shared memory). */
+ * (256, 1024, 4096), the binning CTAs (1 or 2 per SM, within options.binning_ctas) and the
+ * per-bin raster path (options.light_max_pixel: -1, 32, 64, 128, 256; bins up to that depth are
+ * rastered one warp per row, deeper ones by CTA-wide depth windows); CUDA events on `stream`,
+ * median of 3 frames after one warm-up frame each. The winner is stored in the renderer's
+ * options and returned in *out (may be NULL). Synchronous. Bin size is fixed at 32 (the
+ * reference's only enabled size); raster CTAs are one per SM (shared memory). */
 lucid_status lucid_autotune(lucid_renderer* renderer, const lucid_frame_inputs* inputs,
 							float* scratch_rgba, lucid_tuning* out, void* stream);
 
@@ -480,8 +489,8 @@ lucid_status lucid_quad_generate(const float* positions, int32_t num_verts, cons
  * tri_scan (2*max_visible_quads records of 8 u32, LUCID_BUF_TRI_SCAN, 16-byte aligned) of a
  * quad setup with num_small_quads / num_large_quads visible quads.
  * Outputs (device): bin_counters (10 * bin count u32, the g_counts layout), bin_quads and
- * bin_tris (max_bin_refs u32 each), optional info_out (one lucid_info: level counts, error
- * code).
+ * bin_tris (max_bin_refs u32 each; every bin's references in slot order, as with
+ * LUCID_OPT_SORTED_BIN_LISTS), optional info_out (one lucid_info: level counts, error code).
  * Limit: at most LUCID_NOALLOC_MAX_BINS 32x32 bins (e.g. 1920x1080 = 2040 bins); larger
  * viewports return LUCID_CAPACITY_EXCEEDED. All calls share the static scratch: calls whose
  * work overlaps on the GPU race; calls on one stream are ordered. The first call on each

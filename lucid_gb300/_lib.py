@@ -23,7 +23,7 @@ ERR_NAMES = {0: "none", 1: "visible quads", 2: "bin refs", 3: "band entries",
 
 # render option flags
 OPT_TIMERS, OPT_ADDITIVE_BLENDING, OPT_ALPHA_THRESHOLD, OPT_VISUALIZE_ERRORS = 1, 2, 4, 8
-OPT_PIXEL_BLEND, OPT_REFERENCE_ORDER = 16, 32
+OPT_PIXEL_BLEND, OPT_REFERENCE_ORDER, OPT_SORTED_BIN_LISTS = 16, 32, 64
 
 # internal buffers of lucid_download_buffer
 BUF_QUAD_AABBS, BUF_TRI_BARY, BUF_TRI_SCAN, BUF_TRI_DEPTH, BUF_QUAD_COLORS = 0, 1, 2, 3, 4
@@ -92,7 +92,7 @@ class CameraC(ctypes.Structure):
 class Tuning(ctypes.Structure):
     _fields_ = [("pixel_blend", c_uint32), ("low_high_threshold", c_int32), ("binning_ctas", c_int32),
                 ("num_candidates", c_int32), ("frame_ms", ctypes.c_float), ("default_ms", ctypes.c_float),
-                ("reserved", c_int32 * 2)]
+                ("light_max_pixel", c_int32), ("reserved", c_int32 * 1)]
 
 
 class ViewC(ctypes.Structure):

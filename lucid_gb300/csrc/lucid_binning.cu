@@ -13,8 +13,16 @@
 // binDispatchKernel   same CTA ranges as the counter; each CTA reserves its slice of every bin
 //                     once (atomicAdd on *_OFFSETS_TEMP) and scatters quad / tri references.
 //
-// The order of references inside one bin depends on shared-memory atomics (as in the
-// reference); every consumer is order-independent and tests compare lists per bin sorted.
+// binSortKernel       (LUCID_OPT_SORTED_BIN_LISTS) one CTA per bin: each bin's quad and tri
+//                     reference lists in slot order, so that a frame's bin lists are
+//                     reproducible bit for bit. Without it the order inside a bin depends on
+//                     the CTAs' reservations (atomics, as in the reference); no later pass
+//                     depends on it.
+//
+// For small quads (at most 4 bins each) the counter and dispatcher aggregate per warp with
+// __match_any_sync: lanes whose quad touches the same bin add to it with one shared atomic and
+// take consecutive slots of it. Large tris cover very different numbers of rows and bins, so
+// each lane walks its own tri.
 
 #include "lucid_common.cuh"
 #include "lucid_kernels.h"
@@ -64,28 +72,71 @@ __device__ __forceinline__ void ctaRange(int n, int cta, int ncta, int& beg, int
 }
 
 // ---------------------------------------------------------------------------------------------
+// Warp aggregation: lanes holding the same bin (key >= 0) add their count with one shared atomic
+// by the group's lowest lane. Every lane of the warp must call these.
+
+__device__ __forceinline__ void warpAddBin(int* s_bins, int key, int sign) {
+	const uint32_t peers = __match_any_sync(0xffffffffu, key);
+	if(key >= 0 && (threadIdx.x & 31) == __ffs(peers) - 1)
+		atomicAdd(&s_bins[key], sign * __popc(peers));
+}
+
+// Slot of this lane's reference to bin `key` (>= 0): the group's lowest lane reserves the group's
+// slots with one shared atomic; lanes take them in lane order.
+__device__ __forceinline__ uint32_t warpBinSlot(int* s_bins, int key) {
+	const uint32_t peers = __match_any_sync(0xffffffffu, key);
+	const int leader = __ffs(peers) - 1;
+	int base = 0;
+	if(key >= 0 && (threadIdx.x & 31) == leader)
+		base = atomicAdd(&s_bins[key], __popc(peers));
+	base = __shfl_sync(0xffffffffu, base, leader);
+	return uint32_t(base + __popc(peers & laneMaskLt()));
+}
+
+// Bin j (0..3) of a small quad's bin AABB (at most 4 bins, bin_counter.glsl:64-80), -1 if none.
+__device__ __forceinline__ int smallQuadBin(int x0, int y0, int x1, int y1, int bcx, int j) {
+	const int w = x1 - x0 + 1, n = w * (y1 - y0 + 1);
+	if(j >= n)
+		return -1;
+	return (y0 + j / w) * bcx + x0 + j % w;
+}
+
+// A large quad's tri of work item `it` (2 per quad, large quads counted from the top slot down):
+// its slot and encoded AABB; false when the tri is culled.
+__device__ __forceinline__ bool largeTri(const FrameParams& p, int lbeg, int it, uint32_t& tri, uint32_t& enc) {
+	const int k = lbeg + (it >> 1), second = it & 1;
+	const int quad_idx = (p.max_visible_quads - 1) - k;
+	enc = p.quad_aabbs[quad_idx];
+	tri = uint32_t(quad_idx) * 2 + second;
+	return ((enc >> (30 + second)) & 1u) == 0u;
+}
+
+// ---------------------------------------------------------------------------------------------
 
 template <class Src> __global__ void __launch_bounds__(kBinningThreads, 1) binCountKernel(Src src) {
 	extern __shared__ int s_bins[];
 	int cta, ncta;
 	const FrameParams& p = src.get(cta, ncta);
 	const int bins = p.bin_count, bcx = p.bin_count_x, bcy = p.bin_count_y;
-	const int mvq = p.max_visible_quads;
 	const int nsmall = p.info->num_visible_quads[0], nlarge = p.info->num_visible_quads[1];
 	int* hist = p.bin_batches + size_t(cta) * 2 * bins;
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
-	// ---- small quads: every bin of the AABB (bin_counter.glsl:64-80)
+	// ---- small quads: every bin of the AABB (bin_counter.glsl:64-80), one shared atomic per
+	// distinct bin of a warp
 	for(int i = threadIdx.x; i < bins; i += blockDim.x)
 		s_bins[i] = 0;
 	__syncthreads();
 	int sbeg, send;
 	ctaRange(nsmall, cta, ncta, sbeg, send);
-	for(int k = sbeg + threadIdx.x; k < send; k += blockDim.x) {
-		int x0, y0, x1, y1;
-		decodeAABB28(p.quad_aabbs[k], x0, y0, x1, y1);
-		for(int by = y0; by <= y1; by++)
-			for(int bx = x0; bx <= x1; bx++)
-				atomicAdd(&s_bins[by * bcx + bx], 1);
+	for(int base = sbeg + warp * 32; base < send; base += blockDim.x) {
+		const int k = base + lane;
+		int x0 = 0, y0 = 0, x1 = -1, y1 = -1;
+		if(k < send)
+			decodeAABB28(p.quad_aabbs[k], x0, y0, x1, y1);
+		const int nb = __reduce_max_sync(0xffffffffu, (x1 - x0 + 1) * (y1 - y0 + 1));
+		for(int j = 0; j < nb; j++)
+			warpAddBin(s_bins, k < send ? smallQuadBin(x0, y0, x1, y1, bcx, j) : -1, 1);
 	}
 	__syncthreads();
 	for(int i = threadIdx.x; i < bins; i += blockDim.x) {
@@ -96,25 +147,22 @@ template <class Src> __global__ void __launch_bounds__(kBinningThreads, 1) binCo
 	}
 	__syncthreads();
 
-	// ---- large tris: bin rows by scanline (bin_counter.glsl:112-134)
+	// ---- large tris: bin rows by scanline (bin_counter.glsl:112-134) as +1 / -1 difference
+	// arrays (rows per tri vary widely: one lane per tri, shared atomics)
 	for(int i = threadIdx.x; i < bins; i += blockDim.x)
 		s_bins[i] = 0;
 	__syncthreads();
 	int lbeg, lend;
 	ctaRange(nlarge, cta, ncta, lbeg, lend);
-	int items = 2 * (lend - lbeg);
+	const int items = 2 * (lend - lbeg);
 	for(int it = threadIdx.x; it < items; it += blockDim.x) {
-		int k = lbeg + (it >> 1), second = it & 1;
-		int quad_idx = (mvq - 1) - k;
-		uint32_t enc = p.quad_aabbs[quad_idx];
-		if((enc >> (30 + second)) & 1u)
+		uint32_t tri, enc;
+		if(!largeTri(p, lbeg, it, tri, enc))
 			continue;
-		uint32_t tri = uint32_t(quad_idx) * 2 + second;
 		int x0, y0, x1, y1;
 		decodeAABB28(enc, x0, y0, x1, y1);
 		int bsy, bey;
-		BinScan sc = loadScanlineParamsBin(p.tri_scan[size_t(tri) * 2], p.tri_scan[size_t(tri) * 2 + 1],
-										   bsy, bey);
+		BinScan sc = loadScanlineParamsBin(p.tri_scan[size_t(tri) * 2], p.tri_scan[size_t(tri) * 2 + 1], bsy, bey);
 		for(int by = bsy; by <= bey; by++) {
 			int bmin, bmax;
 			scanlineStep(sc, bmin, bmax);
@@ -129,7 +177,7 @@ template <class Src> __global__ void __launch_bounds__(kBinningThreads, 1) binCo
 	__syncthreads();
 	// close the difference arrays: one warp per bin row (bin_counter.glsl:82-103)
 	{
-		int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+		const int nw = blockDim.x >> 5;
 		for(int by = warp; by < bcy; by += nw) {
 			int prev = 0;
 			for(int base = 0; base < bcx; base += 32) {
@@ -255,12 +303,13 @@ template <class Src> __global__ void __launch_bounds__(kBinningThreads, 1) binDi
 	int cta, ncta;
 	const FrameParams& p = src.get(cta, ncta);
 	const int bins = p.bin_count, bcx = p.bin_count_x;
-	const int mvq = p.max_visible_quads;
 	const uint32_t cap = uint32_t(p.max_bin_refs);
 	const int nsmall = p.info->num_visible_quads[0], nlarge = p.info->num_visible_quads[1];
 	const int* hist = p.bin_batches + size_t(cta) * 2 * bins;
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
-	// ---- small quads (bin_dispatcher.glsl:66-80, 202-232)
+	// ---- small quads (bin_dispatcher.glsl:66-80, 202-232): the CTA reserves its slice of every
+	// bin once; a warp's references to one bin take consecutive slots of it
 	for(int i = threadIdx.x; i < bins; i += blockDim.x) {
 		int v = hist[i];
 		s_bins[i] = v > 0 ? int(atomicAdd(&binQuadOffsetsTemp(p, i), uint32_t(v))) : 0;
@@ -268,21 +317,27 @@ template <class Src> __global__ void __launch_bounds__(kBinningThreads, 1) binDi
 	__syncthreads();
 	int sbeg, send;
 	ctaRange(nsmall, cta, ncta, sbeg, send);
-	for(int k = sbeg + threadIdx.x; k < send; k += blockDim.x) {
-		uint32_t enc = p.quad_aabbs[k];
-		uint32_t entry = uint32_t(k) | (enc & 0xf0000000u);
-		int x0, y0, x1, y1;
-		decodeAABB28(enc, x0, y0, x1, y1);
-		for(int by = y0; by <= y1; by++)
-			for(int bx = x0; bx <= x1; bx++) {
-				uint32_t slot = uint32_t(atomicAdd(&s_bins[by * bcx + bx], 1));
-				if(slot < cap)
-					p.bin_quads[slot] = entry;
-			}
+	for(int base = sbeg + warp * 32; base < send; base += blockDim.x) {
+		const int k = base + lane;
+		int x0 = 0, y0 = 0, x1 = -1, y1 = -1;
+		uint32_t entry = 0u;
+		if(k < send) {
+			const uint32_t enc = p.quad_aabbs[k];
+			entry = uint32_t(k) | (enc & 0xf0000000u);
+			decodeAABB28(enc, x0, y0, x1, y1);
+		}
+		const int nb = __reduce_max_sync(0xffffffffu, (x1 - x0 + 1) * (y1 - y0 + 1));
+		for(int j = 0; j < nb; j++) {
+			const int key = k < send ? smallQuadBin(x0, y0, x1, y1, bcx, j) : -1;
+			const uint32_t slot = warpBinSlot(s_bins, key);
+			if(key >= 0 && slot < cap)
+				p.bin_quads[slot] = entry;
+		}
 	}
 	__syncthreads();
 
-	// ---- large tris (bin_dispatcher.glsl:89-114, 234-258)
+	// ---- large tris (bin_dispatcher.glsl:89-114, 234-258): one lane per tri (rows and spans vary
+	// widely), a shared atomic per reference
 	for(int i = threadIdx.x; i < bins; i += blockDim.x) {
 		int v = hist[bins + i];
 		s_bins[i] = v > 0 ? int(atomicAdd(&binTriOffsetsTemp(p, i), uint32_t(v))) : 0;
@@ -290,19 +345,15 @@ template <class Src> __global__ void __launch_bounds__(kBinningThreads, 1) binDi
 	__syncthreads();
 	int lbeg, lend;
 	ctaRange(nlarge, cta, ncta, lbeg, lend);
-	int items = 2 * (lend - lbeg);
+	const int items = 2 * (lend - lbeg);
 	for(int it = threadIdx.x; it < items; it += blockDim.x) {
-		int k = lbeg + (it >> 1), second = it & 1;
-		int quad_idx = (mvq - 1) - k;
-		uint32_t enc = p.quad_aabbs[quad_idx];
-		if((enc >> (30 + second)) & 1u)
+		uint32_t tri, enc;
+		if(!largeTri(p, lbeg, it, tri, enc))
 			continue;
-		uint32_t tri = uint32_t(quad_idx) * 2 + second;
 		int x0, y0, x1, y1;
 		decodeAABB28(enc, x0, y0, x1, y1);
 		int bsy, bey;
-		BinScan sc = loadScanlineParamsBin(p.tri_scan[size_t(tri) * 2], p.tri_scan[size_t(tri) * 2 + 1],
-										   bsy, bey);
+		BinScan sc = loadScanlineParamsBin(p.tri_scan[size_t(tri) * 2], p.tri_scan[size_t(tri) * 2 + 1], bsy, bey);
 		for(int by = bsy; by <= bey; by++) {
 			int bmin, bmax;
 			scanlineStep(sc, bmin, bmax);
@@ -317,6 +368,108 @@ template <class Src> __global__ void __launch_bounds__(kBinningThreads, 1) binDi
 }
 
 // ---------------------------------------------------------------------------------------------
+// Canonical order of the bin reference lists: the dispatcher's slices come in the order the CTAs
+// reserved them (atomics, as in the reference), so each bin's quad and tri lists are sorted here
+// by slot (quad references by their low 28 bits; the cull flags ride along). Every later pass is
+// order-independent; the sorted lists make a frame's binning bit-reproducible. One CTA per bin:
+// up to 32 references by one warp in registers, up to kSortCap in shared memory, longer lists in
+// place in global memory; all by the same bitonic network whose every step moves the smaller
+// element to the lower index, so indices past the list's end act as +infinity and are skipped.
+
+constexpr int kSortThreads = 256;
+constexpr int kSortCap = 4096;
+
+__device__ __forceinline__ uint32_t refKey(uint32_t v) { return v & 0x0fffffffu; }
+
+// Partner of index i in step (k, j) of the network (merge size k, stride j): the first step of
+// each merge pairs i with its mirror in the k-block, the later ones with i ^ j.
+__device__ __forceinline__ int bitonicPartner(int i, int k, int j) { return j == (k >> 1) ? i ^ (k - 1) : i ^ j; }
+
+template <class Src> __global__ void __launch_bounds__(kSortThreads) binSortKernel(Src src) {
+	__shared__ uint32_t s_v[kSortCap];
+	int cta, ncta;
+	const FrameParams& p = src.get(cta, ncta);
+	const int lane = threadIdx.x & 31;
+	for(int bin = cta; bin < p.bin_count; bin += ncta) {
+		for(int list = 0; list < 2; list++) {
+			const uint32_t n = list == 0 ? binQuadCounts(p, bin) : binTriCounts(p, bin);
+			const uint32_t off = list == 0 ? binQuadOffsets(p, bin) : binTriOffsets(p, bin);
+			if(n <= 1u || uint64_t(off) + n > uint64_t(p.max_bin_refs))
+				continue; // nothing to order, or the lists overflowed (error raised)
+			uint32_t* d = (list == 0 ? p.bin_quads : p.bin_tris) + off;
+			const int cnt = int(n);
+			if(cnt <= 32) {
+				if(threadIdx.x < 32) {
+					uint32_t v = lane < cnt ? d[lane] : 0xffffffffu;
+					for(int k = 2; k <= 32; k <<= 1)
+						for(int j = k >> 1; j > 0; j >>= 1) {
+							const int q = bitonicPartner(lane, k, j);
+							const uint32_t o = __shfl_sync(0xffffffffu, v, q);
+							const bool lower = lane < q;
+							const bool swap = lower ? refKey(o) < refKey(v) : refKey(v) < refKey(o);
+							v = swap ? o : v;
+						}
+					if(lane < cnt)
+						d[lane] = v;
+				}
+			} else if(cnt <= kSortCap) {
+				int P = 64;
+				while(P < cnt)
+					P <<= 1;
+				for(int i = threadIdx.x; i < P; i += kSortThreads)
+					s_v[i] = i < cnt ? d[i] : 0xffffffffu;
+				__syncthreads();
+				for(int k = 2; k <= P; k <<= 1)
+					for(int j = k >> 1; j > 0; j >>= 1) {
+						for(int i = threadIdx.x; i < P; i += kSortThreads) {
+							const int q = bitonicPartner(i, k, j);
+							if(q > i) {
+								const uint32_t a = s_v[i], b = s_v[q];
+								if(refKey(b) < refKey(a))
+									s_v[i] = b, s_v[q] = a;
+							}
+						}
+						__syncthreads();
+					}
+				for(int i = threadIdx.x; i < cnt; i += kSortThreads)
+					d[i] = s_v[i];
+			} else {
+				int P = 1;
+				while(P < cnt)
+					P <<= 1;
+				for(int k = 2; k <= P; k <<= 1)
+					for(int j = k >> 1; j > 0; j >>= 1) {
+						for(int i = threadIdx.x; i < cnt; i += kSortThreads) {
+							const int q = bitonicPartner(i, k, j);
+							if(q > i && q < cnt) {
+								const uint32_t a = d[i], b = d[q];
+								if(refKey(b) < refKey(a))
+									d[i] = b, d[q] = a;
+							}
+						}
+						__syncthreads();
+					}
+			}
+			__syncthreads();
+		}
+	}
+}
+
+// ---------------------------------------------------------------------------------------------
+
+cudaError_t configureBinningKernels() {
+	// the counter and dispatcher keep one int per bin of the view in shared memory
+	const int bytes = kMaxBinCount * int(sizeof(int));
+	cudaError_t err;
+	if((err = cudaFuncSetAttribute(binCountKernel<OneView>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) !=
+		   cudaSuccess ||
+	   (err = cudaFuncSetAttribute(binDispatchKernel<OneView>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) !=
+		   cudaSuccess ||
+	   (err = cudaFuncSetAttribute(binCountKernel<BatchViews>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)) !=
+		   cudaSuccess)
+		return err;
+	return cudaFuncSetAttribute(binDispatchKernel<BatchViews>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
 
 void launchBinCount(const FrameParams& p, cudaStream_t stream) {
 	binCountKernel<<<p.num_binning_ctas, kBinningThreads, p.bin_count * sizeof(int), stream>>>(OneView{p});
@@ -326,15 +479,19 @@ void launchBinCategorize(const FrameParams& p, cudaStream_t stream) {
 }
 void launchBinDispatch(const FrameParams& p, cudaStream_t stream) {
 	binDispatchKernel<<<p.num_binning_ctas, kBinningThreads, p.bin_count * sizeof(int), stream>>>(OneView{p});
+	if(p.flags & LUCID_OPT_SORTED_BIN_LISTS)
+		binSortKernel<<<p.bin_count, kSortThreads, 0, stream>>>(OneView{p});
 }
 
-void launchBinningBatch(const BatchViews& per_view, const BatchViews& binning_ctas, int max_bins,
-						cudaStream_t stream) {
+void launchBinningBatch(const BatchViews& per_view, const BatchViews& binning_ctas, const BatchViews& bin_ctas,
+						int max_bins, bool sorted_lists, cudaStream_t stream) {
 	const int n = binning_ctas.cta_off[binning_ctas.num_views];
 	const size_t smem = size_t(max_bins) * sizeof(int);
 	binCountKernel<<<n, kBinningThreads, smem, stream>>>(binning_ctas);
 	binCategorizeKernel<<<per_view.num_views, 1024, 0, stream>>>(per_view);
 	binDispatchKernel<<<n, kBinningThreads, smem, stream>>>(binning_ctas);
+	if(sorted_lists)
+		binSortKernel<<<bin_ctas.cta_off[bin_ctas.num_views], kSortThreads, 0, stream>>>(bin_ctas);
 }
 
 } // namespace lucid

@@ -187,9 +187,10 @@ void setShadingInputs(FrameParams& p, const lucid_frame_inputs* in) {
 // fragments per unfinished pixel that a depth slab of the raster aims at
 int slabTarget(const lucid_renderer* r) { return r->opts.slab_fragments > 0 ? r->opts.slab_fragments : 180; }
 // deepest pixel of a bin that takes the light raster path (-1: none)
-int lightMaxPixel(const lucid_renderer* r) {
-	return r->opts.light_max_pixel == 0 ? 64 : (r->opts.light_max_pixel < 0 ? -1 : r->opts.light_max_pixel);
+int lightMaxPixel(const lucid_options* o) {
+	return o->light_max_pixel == 0 ? 64 : (o->light_max_pixel < 0 ? -1 : o->light_max_pixel);
 }
+int lightMaxPixel(const lucid_renderer* r) { return lightMaxPixel(&r->opts); }
 
 FrameParams makeParams(lucid_renderer* r, const lucid_frame_inputs* in, float* out) {
 	FrameParams p{};
@@ -448,6 +449,8 @@ extern "C" lucid_status lucid_create(const lucid_options* options, int32_t width
 	err = configureRasterKernel();
 	if(err == cudaSuccess)
 		err = configureRefKernel();
+	if(err == cudaSuccess)
+		err = configureBinningKernels();
 	if(err != cudaSuccess)
 		return bail(cudaFail(err, "configure raster kernels"));
 	int ctas_per_sm = r->opts.raster_ctas_per_sm > 0 ? r->opts.raster_ctas_per_sm : 1;
@@ -986,7 +989,7 @@ struct BatchPlan {
 	std::vector<size_t> info_off;    // byte offset of each view's info block in `infos`
 	std::vector<int> binning_ctas;   // per view, fixed when the plan's buffers are sized
 	size_t info_bytes = 0;
-	BatchViews per_view{}, setup_map{}, binning_map{};
+	BatchViews per_view{}, setup_map{}, binning_map{}, bin_map{};
 	std::vector<void*> allocations;
 	FrameParams* params_dev = nullptr;
 	FrameParams* params_pinned = nullptr;
@@ -1182,7 +1185,7 @@ lucid_status buildBatchPlan(lucid_renderer* r, const lucid_view* views, int n, s
 		return bail(cudaFail(err, "batch stream / event"));
 
 	// CTA maps of the passes
-	BatchViews* maps[3] = {&b->per_view, &b->setup_map, &b->binning_map};
+	BatchViews* maps[4] = {&b->per_view, &b->setup_map, &b->binning_map, &b->bin_map};
 	for(BatchViews* m : maps) {
 		m->views = b->params_dev;
 		m->num_views = n;
@@ -1193,6 +1196,7 @@ lucid_status buildBatchPlan(lucid_renderer* r, const lucid_view* views, int n, s
 		b->per_view.cta_off[v + 1] = v + 1;
 		b->setup_map.cta_off[v + 1] = b->setup_map.cta_off[v] + viewSetupCtas(nq);
 		b->binning_map.cta_off[v + 1] = b->binning_map.cta_off[v] + b->binning_ctas[size_t(v)];
+		b->bin_map.cta_off[v + 1] = b->bin_map.cta_off[v] + viewBins(views[v].width, views[v].height);
 	}
 
 	// record the frame
@@ -1203,7 +1207,8 @@ lucid_status buildBatchPlan(lucid_renderer* r, const lucid_view* views, int n, s
 	cudaMemsetAsync(b->infos, 0, b->info_bytes, cs);
 	cudaMemsetAsync(b->counters, 0, 16, cs);
 	launchSetupBatch(b->per_view, b->setup_map, cs);
-	launchBinningBatch(b->per_view, b->binning_map, b->max_bins, cs);
+	launchBinningBatch(b->per_view, b->binning_map, b->bin_map, b->max_bins,
+					   (r->opts.flags & LUCID_OPT_SORTED_BIN_LISTS) != 0, cs);
 	launchRasterBatch(b->params_dev, n, b->level_prefix, b->counters + 2, r->raster_ctas, cs);
 	cudaGraph_t graph = nullptr;
 	cudaError_t cap_err = cudaStreamEndCapture(cs, &graph);
@@ -1373,6 +1378,15 @@ extern "C" lucid_status lucid_autotune(lucid_renderer* r, const lucid_frame_inpu
 			o.binning_ctas = ctas;
 			st = tryOpts(o);
 		}
+		// 4. per-bin raster path: the deepest pixel of a bin that is rastered one warp per row
+		// (light path) instead of by CTA-wide depth windows (-1: every bin by windows)
+		for(int lm : {-1, 32, 64, 128, 256}) {
+			if(st != LUCID_OK || lm == lightMaxPixel(&best))
+				continue;
+			o = best;
+			o.light_max_pixel = lm;
+			st = tryOpts(o);
+		}
 		r->opts = st == LUCID_OK ? best : saved;
 	}
 	cudaEventDestroy(e0);
@@ -1386,6 +1400,7 @@ extern "C" lucid_status lucid_autotune(lucid_renderer* r, const lucid_frame_inpu
 		out->pixel_blend = (r->opts.flags & LUCID_OPT_PIXEL_BLEND) ? 1u : 0u;
 		out->low_high_threshold = r->opts.low_high_threshold;
 		out->binning_ctas = r->opts.binning_ctas;
+		out->light_max_pixel = lightMaxPixel(r);
 		out->num_candidates = candidates;
 		out->frame_ms = best_ms;
 		out->default_ms = default_ms;

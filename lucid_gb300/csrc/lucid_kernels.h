@@ -14,8 +14,8 @@ void launchBinDispatch(const FrameParams& p, cudaStream_t stream);
 void launchRaster(const FrameParams& p, int num_ctas, cudaStream_t stream, int mode = kRasterForward);
 // Batched frames: one launch per pass for every view (CTA ranges per view in the maps).
 void launchSetupBatch(const BatchViews& per_view, const BatchViews& setup_ctas, cudaStream_t stream);
-void launchBinningBatch(const BatchViews& per_view, const BatchViews& binning_ctas, int max_bins,
-						cudaStream_t stream);
+void launchBinningBatch(const BatchViews& per_view, const BatchViews& binning_ctas, const BatchViews& bin_ctas,
+						int max_bins, bool sorted_lists, cudaStream_t stream);
 void launchRasterBatch(const FrameParams* views_dev, int num_views, int* level_prefix, uint32_t* counter,
 					   int num_ctas, cudaStream_t stream);
 // Pixel-parallel kernels over the fragment store: the plain blend and the differentiable
@@ -29,6 +29,7 @@ void launchRefRaster(const FrameParams& p, uint8_t* plan, cudaStream_t stream);
 int quadGenerate(const float* positions, int num_verts, const int32_t* tris, int num_tris, float square_weight,
 				 uint32_t* out_quads, int* out_num_quads, int* out_num_degenerate, cudaStream_t stream,
 				 std::string& err);
+cudaError_t configureBinningKernels();
 size_t rasterSmemBytes();
 int rasterThreads();
 

@@ -3,7 +3,8 @@
 // Who needs it: code that must not call cudaMalloc/cudaFree, for example a host that hands
 // all device memory to its own allocator up front, or a caller that records work while
 // allocation is not permitted. lucid_bin_noalloc runs the bin counter, categorizer and
-// dispatcher kernels of lucid_binning.cu on caller-provided inputs and outputs; the only
+// dispatcher kernels of lucid_binning.cu, and the sort that puts each bin's reference lists in
+// slot order (in place, no scratch), on caller-provided inputs and outputs; the only
 // memory they need beyond those — the counter kernel's per-CTA bin histograms, the status
 // block and the bin work list — lives in the fixed-size static device array below.
 //
@@ -113,6 +114,7 @@ extern "C" lucid_status lucid_bin_noalloc(const uint32_t* quad_aabbs, const uint
 	p.max_bin_refs = max_bin_refs;
 	p.low_high_threshold = low_high_threshold;
 	p.num_binning_ctas = kNoAllocCtas;
+	p.flags = LUCID_OPT_SORTED_BIN_LISTS; // reference lists in slot order (sorted in place)
 	p.info = info;
 	p.counts = bin_counters;
 	p.quad_aabbs = const_cast<uint32_t*>(quad_aabbs);

@@ -244,7 +244,7 @@ class LucidRenderer:
         check(self.lib.lucid_autotune(self.handle, ctypes.byref(fi), _dptr(scratch), ctypes.byref(t),
                                       _stream_ptr(stream)), "lucid_autotune")
         return {k: getattr(t, k) for k in ("pixel_blend", "low_high_threshold", "binning_ctas",
-                                           "num_candidates", "frame_ms", "default_ms")}
+                                           "light_max_pixel", "num_candidates", "frame_ms", "default_ms")}
 
     def render_batch(self, frames, outs=None, stream=None):
         """Renders every (frame, width, height) of `frames` with lucid_render_batch; returns the

@@ -103,7 +103,7 @@ def _shading_inputs(scene, keep):
 def run(scene, max_visible_quads: int | None = None, raster: bool = True, image64: bool = False,
         bin_subset=None, threads: int = 1, max_per_pixel: int = 0, flags: int = 0,
         low_high_threshold: int = 1024, setup_outputs: bool = True, order_mode: int = 0,
-        dump_by_subset: bool = False):
+        dump_by_subset: bool = False, bin_ref_capacity: int | None = None):
     """Runs the oracle on a ``lucid_gb300.scenes.Scene``; returns a dict of numpy arrays.
 
     With ``bin_subset`` and ``dump_by_subset`` (exact order only) the fragment counts and
@@ -133,7 +133,7 @@ def run(scene, max_visible_quads: int | None = None, raster: bool = True, image6
         out["tri_depth"] = np.zeros((2 * mvq, 4), np.uint32)
         out["tri_normals"] = np.zeros(2 * mvq, np.uint32)
     out["bin_counters"] = np.zeros(10 * bins, np.uint32)
-    cap = int(8 * scene.num_quads + 1024)
+    cap = int(8 * scene.num_quads + 1024) if bin_ref_capacity is None else int(bin_ref_capacity)
     out["bin_quads"] = np.zeros(cap, np.uint32)
     out["bin_tris"] = np.zeros(cap, np.uint32)
     compact = dump_by_subset and subset is not None and order_mode == 0
@@ -168,7 +168,11 @@ def run(scene, max_visible_quads: int | None = None, raster: bool = True, image6
         raise RuntimeError(f"oracle_run failed ({rc})")
     nbq, nbt = int(outs.num_bin_quads), int(outs.num_bin_tris)
     if nbq > cap or nbt > cap:
-        raise RuntimeError("oracle bin reference capacity exceeded")
+        if bin_ref_capacity is not None:
+            raise RuntimeError("oracle bin reference capacity exceeded")
+        # the counts are complete: run again with lists of the needed size
+        return run(scene, max_visible_quads, raster, image64, bin_subset, threads, max_per_pixel, flags,
+                   low_high_threshold, setup_outputs, order_mode, dump_by_subset, bin_ref_capacity=max(nbq, nbt))
     out["bin_quads"] = out["bin_quads"][:nbq]
     out["bin_tris"] = out["bin_tris"][:nbt]
     out.update(

@@ -81,7 +81,9 @@ def compare_full_frame_records(scene, g_renderer, oracle_out, info, counters):
 def sampled_parity(scene, oracle, name, n_uniform=40, n_dense=8, max_per_pixel=256, seed=0):
     from lucid_gb300.renderer import FrameInputs, LucidRenderer
     nq = scene.num_quads
-    r = LucidRenderer(scene.width, scene.height, max_input_quads=nq, max_visible_quads=nq, max_bin_refs=8 * nq)
+    from lucid_gb300 import _lib
+    r = LucidRenderer(scene.width, scene.height, max_input_quads=nq, max_visible_quads=nq, max_bin_refs=8 * nq,
+                      flags=_lib.OPT_SORTED_BIN_LISTS)
     frame = FrameInputs.from_scene(scene)
     # binning first (cheap on the CPU) to choose the sample
     ob = oracle.run(scene, max_visible_quads=nq, raster=False)

@@ -3,8 +3,10 @@
 Integer outputs (setup records, bin counts, offsets, bin lists, level lists, per-pixel
 fragment lists and their order) must be bit-exact; images must agree within 1e-5 per channel
 (in practice they are bit-identical: both sides evaluate the same IEEE float expressions).
-Bin lists are compared per bin after sorting, because the order inside a bin comes from
-atomics, as in the reference.
+Bin reference lists are compared bit for bit with LUCID_OPT_SORTED_BIN_LISTS (a per-bin sort
+pass puts every bin's lists in slot order, the oracle's order), and per bin as sets on
+renderers without it (the dispatcher's order inside a bin follows its atomics, as in the
+reference).
 """
 import math
 
@@ -25,7 +27,8 @@ def gpu_run(scene, max_visible_quads=None, flags=0, band_capacity=None, max_bin_
     from lucid_gb300 import _lib
     mvq = max_visible_quads or max(1024, scene.num_quads)
     r = renderer or LucidRenderer(scene.width, scene.height, max_input_quads=max(1024, scene.num_quads),
-                                  max_visible_quads=mvq, flags=flags, band_capacity=band_capacity,
+                                  max_visible_quads=mvq, flags=flags | _lib.OPT_SORTED_BIN_LISTS,
+                                  band_capacity=band_capacity,
                                   max_bin_refs=max_bin_refs or max(1 << 16, 8 * scene.num_quads))
     frame = FrameInputs.from_scene(scene)
     res = {}
@@ -53,9 +56,9 @@ def gpu_run(scene, max_visible_quads=None, flags=0, band_capacity=None, max_bin_
 
 
 def compare(scene, oracle, *, max_visible_quads=None, flags=0, dump=0, check_image=True,
-            renderer=None):
+            renderer=None, image64=True):
     mvq = max_visible_quads or max(1024, scene.num_quads)
-    o = oracle.run(scene, max_visible_quads=mvq, flags=flags, max_per_pixel=dump, image64=True)
+    o = oracle.run(scene, max_visible_quads=mvq, flags=flags, max_per_pixel=dump, image64=image64)
     g = gpu_run(scene, max_visible_quads=mvq, flags=flags, dump=dump, renderer=renderer)
     info = g["info"]
     # ---- setup
@@ -86,13 +89,10 @@ def compare(scene, oracle, *, max_visible_quads=None, flags=0, dump=0, check_ima
     assert tuple(info.bin_level_counts) == tuple(lv)
     np.testing.assert_array_equal(gc[7 * n:7 * n + lv[2]], oc[7 * n:7 * n + lv[2]], err_msg="LOW bins")
     np.testing.assert_array_equal(gc[9 * n:9 * n + lv[4]], oc[9 * n:9 * n + lv[4]], err_msg="HIGH bins")
-    gq = helpers.canonical_quad_lists(gc, n, g["bin_quads"])
-    oq = helpers.canonical_quad_lists(oc, n, o["bin_quads"])
-    gt = helpers.canonical_tri_lists(gc, n, g["bin_tris"])
-    ot = helpers.canonical_tri_lists(oc, n, o["bin_tris"])
-    for b in range(n):
-        np.testing.assert_array_equal(gq[b], oq[b], err_msg=f"bin {b} quads")
-        np.testing.assert_array_equal(gt[b], ot[b], err_msg=f"bin {b} tris")
+    from lucid_gb300 import _lib
+    sorted_lists = bool(g["renderer"].options.flags & _lib.OPT_SORTED_BIN_LISTS)
+    helpers.assert_bin_lists_equal(gc, n, g["bin_quads"], g["bin_tris"], oc, o["bin_quads"], o["bin_tris"],
+                                   exact=sorted_lists)
     # ---- raster
     assert info.num_fragments == o["num_fragments"]
     assert info.num_hblock_tris == o["num_hblock_tris"]
@@ -284,3 +284,12 @@ def test_cpu720_full(gpu, oracle):
     sc = scenes.workload("cpu720")
     g, o = compare(sc, oracle)
     print("fragments", o["num_fragments"], "max/pixel", o["max_pixel_fragments"])
+
+
+def test_largest_viewport(gpu, oracle):
+    """4096x4096, the largest viewport (16384 bins): the bin counter and dispatcher keep one
+    int per bin in shared memory (64 KB, above the default 48 KB limit)."""
+    sc = scenes.random_tris(4096, 4096, 3000, seed=17, area_median=2000.0, area_sigma=1.0,
+                            large_fraction=0.02, large_area=(50000.0, 100000.0))
+    g, o = compare(sc, oracle, image64=False)
+    assert o["bin_count"] == 16384 and o["num_visible"][1] > 0

@@ -4,10 +4,10 @@ not allowed). Its scratch is a static device array shared by all calls.
 
 The test feeds it the quad-setup records of two different scenes in a row (through the C ABI,
 on caller-owned buffers) and checks both results against the regular binning passes of
-lucid_render on the same records: counts, offsets, LOW/HIGH lists bit-exact, reference lists
-equal per bin as sorted sets (their order inside a bin comes from atomics). A second call must
-not see state left by the first. This file is collected last so that a failure here does not
-hide results of the other tests; it also passes alone in a fresh process.
+lucid_render on the same records (with LUCID_OPT_SORTED_BIN_LISTS, the slot order this entry
+point always produces): counts, offsets, LOW/HIGH lists and the reference lists bit-exact. A second call must not see state left by the first. This file is collected last so
+that a failure here does not hide results of the other tests; it also passes alone in a fresh
+process.
 """
 import ctypes
 
@@ -24,7 +24,7 @@ def regular_binning(scene, mvq, cap):
     from lucid_gb300 import _lib
     from lucid_gb300.renderer import FrameInputs, LucidRenderer
     r = LucidRenderer(scene.width, scene.height, max_input_quads=max(1024, scene.num_quads),
-                      max_visible_quads=mvq, max_bin_refs=cap)
+                      max_visible_quads=mvq, max_bin_refs=cap, flags=_lib.OPT_SORTED_BIN_LISTS)
     r.render(FrameInputs.from_scene(scene))
     info, counters = r.info()
     res = dict(info=info, counters=counters,
@@ -66,13 +66,7 @@ def check_same(ref, counters, bq, bt, info, bins):
     np.testing.assert_array_equal(counters[7 * bins:7 * bins + lv[2]], ref["counters"][7 * bins:7 * bins + lv[2]])
     np.testing.assert_array_equal(counters[9 * bins:9 * bins + lv[4]], ref["counters"][9 * bins:9 * bins + lv[4]])
     assert info.error_code == 0
-    gq = helpers.canonical_quad_lists(counters, bins, bq)
-    rq = helpers.canonical_quad_lists(ref["counters"], bins, ref["bin_quads"])
-    gt = helpers.canonical_tri_lists(counters, bins, bt)
-    rt = helpers.canonical_tri_lists(ref["counters"], bins, ref["bin_tris"])
-    for b in range(bins):
-        np.testing.assert_array_equal(gq[b], rq[b])
-        np.testing.assert_array_equal(gt[b], rt[b])
+    helpers.assert_bin_lists_equal(counters, bins, bq, bt, ref["counters"], ref["bin_quads"], ref["bin_tris"])
 
 
 def test_no_alloc_binning_matches_regular_path_twice(gpu, lucid_lib):
