@@ -59,6 +59,10 @@ def parse_args():
     ap.add_argument("--workload", default=WORKLOAD,
                     help="scenes.workload name (the default is the benchmark workload; smaller "
                          "ones exist for profiler captures)")
+    ap.add_argument("--frames-only", type=int, default=0,
+                    help="profiler captures: render this many frames of --workload (or, with "
+                         "--workload batch64, of the 64-view batch) through the public API and "
+                         "exit, with no timing")
     return ap.parse_args()
 
 
@@ -488,11 +492,40 @@ def profile_figures():
     return res
 
 
+def frames_only(args):
+    """Renders args.frames_only frames and returns (for ncu captures of a known launch list)."""
+    import torch
+    from lucid_gb300 import build as lucid_build
+    lucid_build.build()
+    from lucid_gb300 import scenes
+    from lucid_gb300.renderer import FrameInputs, LucidRenderer
+    if args.workload == "batch64":
+        views = scenes.batch_views(64)
+        frames = [(FrameInputs.from_scene(v), v.width, v.height) for v in views]
+        nq = sum(max(1, v.num_quads) for v in views)
+        r = LucidRenderer(max(v.width for v in views), max(v.height for v in views), max_input_quads=nq,
+                          max_visible_quads=nq, max_bin_refs=4 * nq, max_views=64)
+        for _ in range(args.frames_only):
+            r.render_batch(frames)
+    else:
+        sc = scenes.workload(args.workload)
+        r = LucidRenderer(sc.width, sc.height, max_input_quads=sc.num_quads, max_visible_quads=sc.num_quads,
+                          max_bin_refs=8 * sc.num_quads)
+        frame, out = FrameInputs.from_scene(sc), r.new_image()
+        for _ in range(args.frames_only):
+            r.render(frame, out)
+    torch.cuda.synchronize()
+    r.close()
+
+
 def main():
     args = parse_args()
     rank, world, local = dist_setup(args.gpus)
     if args.impl == "reference":
         run_reference(args, rank)
+        return
+    if args.frames_only > 0:
+        frames_only(args)
         return
 
     import torch
