@@ -119,3 +119,19 @@ def test_batch_topology_change_and_limits(gpu):
         small.render_batch(f[:1] + f[3:4])  # quads beyond the renderer's capacity / size
     assert e.value.status in (_lib.CAPACITY_EXCEEDED, _lib.INVALID_ARG)
     small.close()
+
+
+def test_batch_views_match_oracle(gpu, oracle):
+    """The batch against the CPU oracle directly (not only against single-view GPU renders):
+    every view's image within 1e-5 and its fragment and visible-quad counts equal."""
+    from lucid_gb300.renderer import FrameInputs
+    views = _mixed_views()
+    r = _batch_renderer(views)
+    imgs = r.render_batch([(FrameInputs.from_scene(v), v.width, v.height) for v in views])
+    for i, sc in enumerate(views):
+        o = oracle.run(sc, max_visible_quads=max(1024, sc.num_quads), setup_outputs=False)
+        assert np.abs(imgs[i].cpu().numpy() - o["image"]).max() <= 1e-5, i
+        info = r.batch_info(i)
+        assert int(info.num_fragments) == o["num_fragments"], i
+        assert tuple(info.num_visible_quads) == tuple(o["num_visible"]), i
+    r.close()
