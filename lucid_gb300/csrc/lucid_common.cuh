@@ -72,8 +72,8 @@ struct FrameParams {
 	uint4* quad_colors;
 	uint4* quad_normals;  // encoded vertex normals per quad slot (STORAGE_QUAD_NORMAL)
 	uint4* quad_tex;      // 2 per quad slot: tex0, tex1 - tex0, tex2 - tex0, tex3 - tex0
-	uint4* tri_bary;  // 2 per tri
-	uint4* tri_shade; // shadeRecWords(color_format) per tri: the two tri_bary records, then the vertex
+	uint4* tri_shade; // shadeRecWords(color_format) per tri: the two bary records (edge planes and
+	                  // bary parameters, quad_setup.glsl:290-309), then the vertex
 	                  // colours (RGBA8 or FP16, when the instance has them) and its instance
 	                  // flags | id << 16 (ShadeRec in lucid_shade.cuh)
 	uint4* tri_scan;  // 2 per tri

@@ -85,7 +85,6 @@ struct lucid_renderer {
 	uint4* quad_colors = nullptr;
 	uint4* quad_normals = nullptr;
 	uint4* quad_tex = nullptr;
-	uint4* tri_bary = nullptr;
 	uint4* tri_shade = nullptr;
 	uint4* tri_scan = nullptr;
 	uint4* tri_depth = nullptr;
@@ -230,7 +229,6 @@ FrameParams makeParams(lucid_renderer* r, const lucid_frame_inputs* in, float* o
 	p.quad_colors = r->quad_colors;
 	p.quad_normals = r->quad_normals;
 	p.quad_tex = r->quad_tex;
-	p.tri_bary = r->tri_bary;
 	p.tri_shade = r->tri_shade;
 	p.tri_scan = r->tri_scan;
 	p.tri_depth = r->tri_depth;
@@ -471,7 +469,6 @@ extern "C" lucid_status lucid_create(const lucid_options* options, int32_t width
 	   (st = allocate(r, &r->quad_colors, mvq)) != LUCID_OK ||
 	   (st = allocate(r, &r->quad_normals, mvq)) != LUCID_OK ||
 	   (st = allocate(r, &r->quad_tex, 2 * mvq)) != LUCID_OK ||
-	   (st = allocate(r, &r->tri_bary, 4 * mvq)) != LUCID_OK ||
 	   (st = allocate(r, &r->tri_shade, 2 * kShadeRecWords * mvq)) != LUCID_OK ||
 	   (st = allocate(r, &r->tri_scan, 4 * mvq)) != LUCID_OK ||
 	   (st = allocate(r, &r->tri_depth, 2 * mvq)) != LUCID_OK ||
@@ -490,7 +487,7 @@ extern "C" lucid_status lucid_create(const lucid_options* options, int32_t width
 		cudaMemset(p, 0, mvq * 4);
 	cudaMemset(r->quad_verts, 0, mvq * 16);
 	cudaMemset(r->quad_colors, 0, mvq * 16);
-	cudaMemset(r->tri_bary, 0, mvq * 64);
+	cudaMemset(r->tri_shade, 0, mvq * 2 * kShadeRecWords * 16);
 	cudaMemset(r->tri_scan, 0, mvq * 64);
 	cudaMemset(r->tri_depth, 0, mvq * 32);
 	cudaMemset(r->tri_normals, 0, mvq * 8);
@@ -687,7 +684,9 @@ extern "C" lucid_status lucid_download_buffer(lucid_renderer* r, int32_t which, 
 	size_t size = 0;
 	switch(which) {
 	case LUCID_BUF_QUAD_AABBS: src = r->quad_aabbs, size = mvq * 4; break;
-	case LUCID_BUF_TRI_BARY: src = r->tri_bary, size = mvq * 64; break;
+	case LUCID_BUF_TRI_BARY: // the first 32 bytes of every tri's shading record
+		src = r->tri_shade, size = mvq * 64;
+		break;
 	case LUCID_BUF_TRI_SCAN: src = r->tri_scan, size = mvq * 64; break;
 	case LUCID_BUF_TRI_DEPTH: src = r->tri_depth, size = mvq * 32; break;
 	case LUCID_BUF_QUAD_COLORS: src = r->quad_colors, size = mvq * 16; break;
@@ -702,7 +701,14 @@ extern "C" lucid_status lucid_download_buffer(lucid_renderer* r, int32_t which, 
 		*out_bytes = size;
 	if(host_dst && bytes) {
 		LUCID_CUDA_TRY(cudaStreamSynchronize(reinterpret_cast<cudaStream_t>(stream)));
-		LUCID_CUDA_TRY(cudaMemcpy(host_dst, src, std::min(bytes, size), cudaMemcpyDeviceToHost));
+		if(which == LUCID_BUF_TRI_BARY) {
+			const size_t pitch = size_t(shadeRecWords(r->last.color_format)) * 16;
+			const size_t rows = std::min(bytes, size) / 32;
+			if(rows)
+				LUCID_CUDA_TRY(cudaMemcpy2D(host_dst, 32, src, pitch, 32, rows, cudaMemcpyDeviceToHost));
+		} else {
+			LUCID_CUDA_TRY(cudaMemcpy(host_dst, src, std::min(bytes, size), cudaMemcpyDeviceToHost));
+		}
 	}
 	return LUCID_OK;
 }
@@ -1110,7 +1116,6 @@ void batchParams(lucid_renderer* r, BatchPlan* b, const lucid_view* views, std::
 		p.quad_colors = r->quad_colors + qbase;
 		p.quad_normals = r->quad_normals + qbase;
 		p.quad_tex = r->quad_tex + 2 * qbase;
-		p.tri_bary = r->tri_bary + 4 * qbase;
 		p.tri_shade = r->tri_shade + 2 * kShadeRecWords * qbase;
 		p.tri_scan = r->tri_scan + 4 * qbase;
 		p.tri_depth = r->tri_depth + 2 * qbase;

@@ -515,7 +515,25 @@ __device__ unsigned long long lightRow(const FrameParams& p, const RasterSmem& s
 				const float4 d = planes[size_t(b) * band_cap + j];
 				const uint32_t t = entryTri(e);
 				const float ty = d.y * fy + d.z;
-				for(int x = lo; x <= hi; x++) {
+				int x = lo;
+				// four cursors reserved before any of their stores: the atomics' latencies overlap
+				for(; x + 3 <= hi; x += 4) {
+					uint32_t key[4];
+					int pos[4];
+#pragma unroll
+					for(int u = 0; u < 4; u++)
+						key[u] = nearFirstKey(d.x * float(bin_x + x + u) + ty);
+#pragma unroll
+					for(int u = 0; u < 4; u++)
+						pos[u] = atomicAdd(&cursor[x + u], 1);
+#pragma unroll
+					for(int u = 0; u < 4; u++)
+						if(pos[u] < kLightPool) {
+							K[pos[u]] = key[u];
+							V[pos[u]] = t;
+						}
+				}
+				for(; x <= hi; x++) {
 					const uint32_t key = nearFirstKey(d.x * float(bin_x + x) + ty);
 					const int pos = atomicAdd(&cursor[x], 1);
 					if(pos < kLightPool) {

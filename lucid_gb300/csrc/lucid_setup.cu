@@ -235,8 +235,6 @@ __device__ __forceinline__ void storeTri(const FrameParams& p, const lucid_confi
 	p.tri_depth[tri_idx] = make_uint4(fbits(deq.x), fbits(deq.y), fbits(deq.z), inst_flags_id);
 	const uint4 bary0 = make_uint4(fbits(e0.x), fbits(e0.y), fbits(e0.z), fbits(param0));
 	const uint4 bary1 = make_uint4(fbits(e1.x), fbits(e1.y), fbits(e1.z), fbits(param1));
-	p.tri_bary[size_t(tri_idx) * 2 + 0] = bary0;
-	p.tri_bary[size_t(tri_idx) * 2 + 1] = bary1;
 	// the shading record: what a fragment of the tri reads, in 48 (64 with FP16 colours)
 	// contiguous bytes (layout: ShadeRec in lucid_shade.cuh)
 	uint4* rec = p.tri_shade + size_t(tri_idx) * shadeRecWords(p.color_format);
