@@ -8,7 +8,8 @@ RGBA8, alpha U[0.1, 0.9]), exact per-pixel order, FP32 RGBA output. A step is on
 value      fragments/s with the scene resident in device memory (CUDA events around each step
            on the launching stream; L2 flushed by a 256 MB write between steps).
 e2e        same metric through lucid_render with host buffers: every step copies the scene from
-           pinned host memory and reads the FP32 image back.
+           pinned host memory and reads the FP32 image back, as a serving loop (uploads and
+           read-backs on copy streams overlap the neighbouring frames' renders).
 roofline   raster kernel (the dominant kernel): algorithmic bytes per launch / its measured time.
 cpu_baseline  the CPU oracle (port of the reference passes): one whole frame of the workload on
            all host threads (measured), and the 1280x720 / 100k-triangle frame on 1 core and on
@@ -619,22 +620,43 @@ def main():
                 "algorithmic_bytes": alg_bytes, "kernel_ms": raster_ms,
                 "limiter": "issue slots and latency (fragments stay in shared memory)", **profile_figures()}
 
-    # ---- e2e: host buffers through lucid_render
-    host = {k: getattr(frame, k).cpu().pin_memory() for k in
-            ("positions", "colors", "quads", "instances", "instance_colors")}
-    host_out = torch.empty(out.shape, dtype=out.dtype).pin_memory()
+    # ---- e2e: host buffers through lucid_render, as a serving loop: every step uploads its
+    # inputs from pinned host memory and reads its image back; uploads run on one copy stream and
+    # read-backs on another, so they overlap the neighbouring frames' renders (two input and two
+    # image buffers)
+    keys = ("positions", "colors", "quads", "instances", "instance_colors")
+    host = {k: getattr(frame, k).cpu().pin_memory() for k in keys}
+    fbuf = [frame, FrameInputs.from_scene(scene)]
+    obuf = [out, r.new_image()]
+    host_out = [torch.empty(out.shape, dtype=out.dtype).pin_memory() for _ in range(2)]
     h2d = sum(t.numel() * t.element_size() for t in host.values())
-    d2h = host_out.numel() * host_out.element_size()
+    d2h = host_out[0].numel() * host_out[0].element_size()
+    up_stream, down_stream = torch.cuda.Stream(), torch.cuda.Stream()
+    up_done = [torch.cuda.Event() for _ in range(2)]
+    rendered = [torch.cuda.Event() for _ in range(2)]
+    read_back = [torch.cuda.Event() for _ in range(2)]
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     for i in range(args.warmup + args.steps):
+        b = i % 2
         if i == args.warmup:
             torch.cuda.synchronize()
             e0.record(stream)
-        for k, t in host.items():
-            getattr(frame, k).copy_(t, non_blocking=True)
-        r.render(frame, out)
-        host_out.copy_(out, non_blocking=True)
+        up_stream.wait_event(rendered[b])  # frame i-2 has finished reading buffer b
+        with torch.cuda.stream(up_stream):
+            for k in keys:
+                getattr(fbuf[b], k).copy_(host[k], non_blocking=True)
+        up_done[b].record(up_stream)
+        stream.wait_event(up_done[b])
+        stream.wait_event(read_back[b])  # frame i-2's image has been read back
+        r.render(fbuf[b], obuf[b], stream=stream)
+        rendered[b].record(stream)
+        down_stream.wait_event(rendered[b])
+        with torch.cuda.stream(down_stream):
+            host_out[b].copy_(obuf[b], non_blocking=True)
+        read_back[b].record(down_stream)
+    for ev in read_back:
+        stream.wait_event(ev)
     e1.record(stream)
     torch.cuda.synchronize()
     e2e_value, e2e_total_ms, _ = replicas.aggregate(e0.elapsed_time(e1), fragments * args.steps, dist, "cuda")
@@ -664,7 +686,9 @@ def main():
                        "parallelism": f"replicas x{world}"},
             "blended_fragments_per_s": blended * args.steps * world / (total_ms / 1e3),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                    "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms},
+                    "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms,
+                    "pipelining": "uploads and read-backs on two copy streams overlap the "
+                                  "neighbouring frames' renders (two input and image buffers)"},
             "roofline": roofline,
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
