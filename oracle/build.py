@@ -4,8 +4,9 @@ The oracle must use plain IEEE float arithmetic with no FMA contraction so that 
 CUDA path bit for bit: -ffp-contract=off (GCC contracts by default on aarch64), no
 -ffast-math, no -march=native (the same source builds on x86-64 and aarch64).
 
-The reference itself cannot be built into oracle/_ref: its raster path exists only as Vulkan
-GLSL compute shaders and its host code needs the libfwk submodule, which is empty.
+The reference's own setup, bin-counter and row-span shader functions are compiled separately
+into oracle/_ref by oracle/ref_build.py (the pin of this oracle); its raster passes need a
+graphics stack and its host code the libfwk submodule, which is empty.
 """
 import os
 import subprocess

@@ -5,8 +5,8 @@
 // contraction (built with -ffp-contract=off) and the float->int conversion rules of the GPU
 // (saturating, NaN -> 0). Bin lists are produced in canonical order (per bin, by slot).
 //
-// Parity with the reference is unpinned (no runnable reference, no golden vectors); see the
-// header for what pins it instead.
+// Setup, binning counts and per-pixel coverage are pinned to the reference's own shader
+// functions compiled as C++ (oracle/ref_build.py); the header says what pins the rest.
 
 #include "lucid_oracle.h"
 

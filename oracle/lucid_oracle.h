@@ -5,10 +5,14 @@
  * baseline. Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load it.
  * Nothing in the lucid_gb300 package links, imports or calls it.
  *
- * Parity status: UNPINNED against the reference's own outputs. The reference runs only as
- * Vulkan GLSL compute shaders on top of libfwk (absent), and has no tests or golden vectors,
- * so this restatement is checked against hand-derived known-answer cases and invariants of
- * the reference (src/lucid_renderer.cpp:629-707 offset checks) instead.
+ * Parity status: the reference runs only as Vulkan GLSL compute shaders on top of libfwk
+ * (absent) and has no tests or golden vectors. Its setup, bin-counter and low-level row-span
+ * functions are compiled as C++ from its shader sources (oracle/ref_build.py, oracle/_ref), and
+ * this restatement's setup records, per-bin counts and per-pixel fragment counts are checked
+ * bit for bit against them (tests/test_oracle_ref_pin.py). The exact per-pixel order and blend
+ * (an extension of the reference's approximate window) are checked against hand-derived
+ * known-answer cases, the FP64 blend and the reference's run-time invariants
+ * (src/lucid_renderer.cpp:629-707 offset checks).
  *
  * Layout conventions shared with the CUDA path (both follow the reference):
  *   - quad slot k < num_visible[0] holds the k-th visible small quad in input order;
