@@ -19,7 +19,10 @@
 //     first one it has not processed, that holds >= kWindow fragments. Buckets split the key
 //     space in order, so windows visit each pixel's fragments strictly front to back. A slab
 //     covers about slab_target fragments per unfinished pixel (from an estimate gathered with
-//     the group's key range); the next slab is counted only if a pixel needs it.
+//     the group's key range); the next slab is counted only if a pixel needs it. The first
+//     slab is generated directly: one pass over the band entries appends its fragments to
+//     per-pixel regions of the idle sort buffer, the histograms are counted from there, and the
+//     first window is scattered from the regions (no second pass over the entries).
 //  D. Per window: fragments (32-bit nearest-first depth key, 32-bit payload = pixel | tri) are
 //     generated by one warp per pixel row (lane = pixel, band entries broadcast by shuffle) and
 //     written to their pixel's segment, in a heavy group to the sub-segment of their depth
@@ -36,6 +39,25 @@
 #include "lucid_shade.cuh"
 
 namespace lucid {
+
+// Work counters of the depth-window path (diagnostics, off by default): built with
+// LUCID_RASTER_COUNTERS=1 (lucid_gb300/build.py --counters) and run with LUCID_OPT_TIMERS, the
+// kernel adds 24 64-bit counts into lucid_info.temp (read by lucid_gb300/profile_raster.py):
+//  0 key-range entry visits      1 / 2 slab-histogram fragments evaluated / counted
+//  3 / 4 window-generation fragments evaluated / kept   5 / 6 entries broadcast by 1-2 / 3-4
+//  7 slabs built                 8 depth-window groups     9 direct slabs sent to the histogram
+// 10 fragments shaded           11 windows               12 cycles of window selection (thread 0)
+// 13 cycles of window generation (thread 0)              14 cycles of key ranges (thread 0)
+// 15 cycles of the walk (thread 0)                       16 / 17 direct append: warp cycles
+//    summed over warps / wall cycles (thread 0)          18 / 19 walk: warp cycles / wall cycles
+#ifndef LUCID_RASTER_COUNTERS
+#define LUCID_RASTER_COUNTERS 0
+#endif
+#if LUCID_RASTER_COUNTERS
+#define RCOUNT(i, v) (rc[i] += (unsigned long long)(v))
+#else
+#define RCOUNT(i, v) ((void)0)
+#endif
 
 constexpr int RT = kRasterThreads;
 constexpr int NW = RT / 32;
@@ -80,6 +102,7 @@ struct RasterSmem {
 	int px_bcur[kGroupPixels];   // blend cursor
 	int px_done[kGroupPixels];   // fragments already processed (verification dump index)
 	int px_state[kGroupPixels];  // 0 active, 1 finished
+	int px_rend[kGroupPixels];   // fragments of the pixel's region of a directly generated slab
 	// sub-segments of the current window that need sorting, as (start << 16 | count):
 	// counts 2..16 are sorted by one thread, by size class (2, 3-4, 5-8, 9-16; class 0 from the
 	// front and class 2 from the back of sub_small, classes 1 and 3 likewise in `radix`, which
@@ -116,7 +139,14 @@ static_assert(2 * NW * kLightPool <= 4 * kGroupCap, "the light path's row pools 
 // Depth histogram slot of pixel t's bucket bk (2^nb_log >= 32 buckets per pixel). The bucket is
 // XOR-swizzled by the pixel's lane so that the 32 pixels of a row, which mostly hit the same
 // bucket of a planar triangle, fall into 32 different shared-memory banks.
-__device__ __forceinline__ int histIdx(int t, int bk, int nb_log) { return (t << nb_log) | (bk ^ (t & 31)); }
+// With 2^nb_log = 32 << g buckets per pixel, lane l of a pixel's warp owns buckets
+// [l << g, (l + 1) << g): bucket bk sits in plane (bk & (2^g - 1)) of 32 words at column
+// (bk >> g) ^ (t & 31), so a lane's buckets are conflict-free loads across the warp and the 32
+// pixels of a row that hit one bucket still use 32 different banks.
+__device__ __forceinline__ int histIdx(int t, int bk, int nb_log) {
+	const int g = nb_log - 5;
+	return (t << nb_log) | ((bk & ((1 << g) - 1)) << 5) | ((bk >> g) ^ (t & 31));
+}
 
 // A sub-segment of a window to sort: start relative to its pixel's window (13 bits), count
 // (9 bits) and pixel of the group (8 bits).
@@ -350,12 +380,13 @@ __device__ void writePixel(const FrameParams& p, int px, int py, float4 c) {
 // only entries whose range meets the current window of some pixel of the row are visited; the
 // window of pixel t holds the keys of its buckets [px_lo, px_cut] (bucket = (key - kmin) >> shift).
 // With `ekeys` and flo <= fhi, entries are culled against the fixed key range [flo, fhi] instead.
-template <typename Fn>
+template <bool kQuad = false, typename Fn>
 __device__ __forceinline__ void forEachGroupFragment(const FrameParams& p, const RasterSmem& s,
 													  const uint2* scratch, const float4* planes, int band_cap, int bin_x,
 													  int bin_y, int p0, int p1, Fn fn,
 													  const uint2* ekeys = nullptr, uint32_t kmin = 0u,
-													  int shift = 0, uint32_t flo = 1u, uint32_t fhi = 0u) {
+													  int shift = 0, uint32_t flo = 1u, uint32_t fhi = 0u,
+													  unsigned long long* ecount = nullptr) {
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	const int r0 = p0 >> 5, r1 = (p1 - 1) >> 5;
 	const int nrows = r1 - r0 + 1;
@@ -392,21 +423,36 @@ __device__ __forceinline__ void forEachGroupFragment(const FrameParams& p, const
 	}
 	// the group's columns in this row
 	const int glo = max(0, p0 - 32 * row), ghi = min(31, p1 - 1 - 32 * row);
+	// lane j's entry, its key range and plane are loaded together, and the next chunk's while
+	// this one is processed
+	const size_t bbase = size_t(b) * band_cap;
+	uint2 n_e = make_uint2(0u, 0u), n_kr = make_uint2(0u, 0xffffffffu);
+	float4 n_d = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+	if(jbeg + lane < jend) {
+		n_e = scratch[bbase + jbeg + lane];
+		n_d = planes[bbase + jbeg + lane];
+		if(ekeys)
+			n_kr = ekeys[bbase + jbeg + lane];
+	}
 	for(int j0 = jbeg; j0 < jend; j0 += 32) {
 		// lane j's entry: its span in this row, its tri and the row's part of its plane
 		// (dy * py + dz, the same for every pixel of the row); only entries whose span meets
 		// the group's columns take part
 		const int j = j0 + lane;
 		bool rel = j < jend;
-		if(rel && ekeys) {
-			const uint2 kr = ekeys[size_t(b) * band_cap + j];
-			rel = kr.y >= wlo && kr.x <= whi;
+		const uint2 e = n_e, kr = n_kr;
+		const float4 d = n_d;
+		if(j + 32 < jend) {
+			n_e = scratch[bbase + j + 32];
+			n_d = planes[bbase + j + 32];
+			if(ekeys)
+				n_kr = ekeys[bbase + j + 32];
 		}
+		if(rel && ekeys)
+			rel = kr.y >= wlo && kr.x <= whi;
 		uint32_t span = 0u, tri = 0u;
 		float dx = 0.0f, ty = 0.0f;
 		if(rel) {
-			const uint2 e = scratch[size_t(b) * band_cap + j];
-			const float4 d = planes[size_t(b) * band_cap + j];
 			const int lo = (e.x >> rshift) & 31, hi = (e.y >> rshift) & 31;
 			rel = max(lo, glo) <= min(hi, ghi);
 			if(rel) {
@@ -419,6 +465,8 @@ __device__ __forceinline__ void forEachGroupFragment(const FrameParams& p, const
 		// up to four entries per step (in lane order), so that their shuffles, key evaluations and
 		// the callbacks' shared-memory round trips overlap
 		uint32_t todo = __ballot_sync(0xffffffffu, rel);
+		if(LUCID_RASTER_COUNTERS && ecount && lane == 0)
+			*ecount += __popc(todo);
 		while(todo != 0u) {
 			int k[4];
 			bool has[4];
@@ -441,10 +489,20 @@ __device__ __forceinline__ void forEachGroupFragment(const FrameParams& p, const
 #pragma unroll
 			for(int u = 0; u < 4; u++)
 				key[u] = nearFirstKey(kdx[u] * fx + kty[u]);
+			if constexpr(kQuad) {
+				// the four entries' fragments of this lane in one call (the callback can issue
+				// their shared-memory atomics back to back)
+				bool on[4];
 #pragma unroll
-			for(int u = 0; u < 4; u++)
-				if(has[u] && in_group && lane >= int(sp[u] & 31u) && lane <= int(sp[u] >> 5))
-					fn(t, key[u], tr[u]);
+				for(int u = 0; u < 4; u++)
+					on[u] = has[u] && in_group && lane >= int(sp[u] & 31u) && lane <= int(sp[u] >> 5);
+				fn(t, on, key, tr);
+			} else {
+#pragma unroll
+				for(int u = 0; u < 4; u++)
+					if(has[u] && in_group && lane >= int(sp[u] & 31u) && lane <= int(sp[u] >> 5))
+						fn(t, key[u], tr[u]);
+			}
 		}
 	}
 }
@@ -793,6 +851,10 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 	lucid_info* const timer_info = work.timerInfo();
 	const bool timers = (opt_flags & LUCID_OPT_TIMERS) != 0 && timer_info != nullptr;
 	long long tacc[8] = {0, 0, 0, 0, 0, 0, 0, 0}, tlast = timers ? clock64() : 0;
+#if LUCID_RASTER_COUNTERS
+	unsigned long long rc[24] = {};
+	long long tc2 = 0;
+#endif
 #define RASTER_TIMER(i)                                                                            \
 	do {                                                                                           \
 		if(timers && tid == 0) {                                                                   \
@@ -1078,6 +1140,11 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 
 			// C1. key range, fragment estimate and per-pixel depth histograms of a heavy group
 			int nb_log = 0, shift = 0;
+			bool slabs_on = false; // slab 0 is narrower than the group's key range
+#if LUCID_RASTER_COUNTERS
+			if(tid == 0)
+				tc2 = clock64();
+#endif
 			if(windowed) {
 				const int r0 = p0 >> 5, r1 = (p1 - 1) >> 5;
 				// slabs only when the group holds more than two slabs' fragments (a second pass over
@@ -1085,6 +1152,7 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 				const int n_active0 = __syncthreads_count(t < npix && s.px_state[t] != 1);
 				const bool slabs = (unsigned long long)s.group_frags >
 								   2ull * (unsigned long long)max(1, p.slab_target) * (unsigned long long)max(1, n_active0);
+				slabs_on = slabs;
 				if(slabs)
 					for(int i = tid; i < kCoarseBins; i += RT)
 						s.hist[i] = 0u;
@@ -1097,6 +1165,7 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 					for(int j = tid; j < ne; j += RT) {
 						uint2 e = scratch[size_t(b) * band_cap + j];
 						const float4 d = planes[size_t(b) * band_cap + j];
+						RCOUNT(0, 1);
 						float dx = d.x, dy = d.y, dz = d.z;
 						uint32_t emn = 0xffffffffu, emx = 0u;
 						int wsum = 0;
@@ -1201,18 +1270,29 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 				const int sh = shift;
 				// entries are culled against the slab only when it is narrower than the group's keys
 				const bool cull = lo_k > s.kmin || hi_k < s.kmax;
+				RCOUNT(7, tid == 0);
+#if LUCID_RASTER_COUNTERS
+				unsigned long long* ec5 = &rc[5];
+#else
+				unsigned long long* ec5 = nullptr;
+#endif
 				if(cull)
 					forEachGroupFragment(p, s, scratch, planes, band_cap, bin_x, bin_y, p0, p1,
 										 [&](int tp, uint32_t key, uint32_t) {
-											 if(key >= lo_k && key <= hi_k)
+											 RCOUNT(1, 1);
+											 if(key >= lo_k && key <= hi_k) {
+												 RCOUNT(2, 1);
 												 atomicAdd(&s.hist[histIdx(tp, int((key - lo_k) >> sh), nb_log)], 1u);
+											 }
 										 },
-										 ekeys, 0u, 0, lo_k, hi_k);
+										 ekeys, 0u, 0, lo_k, hi_k, ec5);
 				else // the whole key range: no test per fragment
 					forEachGroupFragment(p, s, scratch, planes, band_cap, bin_x, bin_y, p0, p1,
 										 [&](int tp, uint32_t key, uint32_t) {
+											 RCOUNT(1, 1);
+											 RCOUNT(2, 1);
 											 atomicAdd(&s.hist[histIdx(tp, int((key - lo_k) >> sh), nb_log)], 1u);
-										 });
+										 }, nullptr, 0u, 0, 1u, 0u, ec5);
 				__syncthreads();
 				if(t < npix && s.px_state[t] != 1) {
 					s.px_state[t] = 0;
@@ -1220,12 +1300,109 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 				}
 				__syncthreads();
 			};
-			if(windowed)
-				buildSlab(0);
+#if LUCID_RASTER_COUNTERS
+			if(tid == 0)
+				rc[14] += clock64() - tc2;
+#endif
+			// Direct slab 0: one pass over the band entries appends every fragment of the slab to
+			// its pixel's region of the idle sort buffer (kGroupCap / npix fragments per pixel);
+			// the per-pixel bucket counts are then taken from the regions in shared memory, and
+			// the first window is scattered from them instead of generated from the entries
+			// again. A pixel whose slab overflows its region sends the group to the histogram
+			// pass over the entries.
+			// odd region stride: the pixels of a row append at similar cursors, so that their
+			// stores fall into different banks
+			const int rcap = ((kGroupCap / max(npix, 1)) - 1) | 1;
+			bool direct_src = false;
+			auto buildSlabDirect = [&]() -> bool {
+				if(rcap < 64)
+					return false;
+				// a pixel with more fragments than its region fits only if slab 0 is narrower
+				// than the group's keys
+				if(!slabs_on && __syncthreads_or(t < npix && s.pix_count[p0 + t] > rcap))
+					return false;
+				if(tid == 0) {
+					int next = 1;
+					while(next < kMaxSlabs && s.slab_first[next] == 0x7fffffff)
+						next++;
+					s.slab_lo = s.kmin;
+					s.slab_hi = next >= kMaxSlabs ? s.kmax : (uint32_t(s.slab_first[next]) << kCoarseShift) - 1u;
+					s.slab_next = next;
+				}
+				if(t < npix)
+					s.px_wend[t] = t * rcap;
+				__syncthreads();
+				slab_lo = s.slab_lo, slab_hi = s.slab_hi;
+				const uint32_t range = slab_hi - slab_lo;
+				const int bits = range ? 32 - __clz(range) : 0;
+				shift = max(0, bits - nb_log);
+				const uint32_t lo_k = slab_lo, hi_k = slab_hi;
+				const bool cull = lo_k > s.kmin || hi_k < s.kmax;
+#if LUCID_RASTER_COUNTERS
+				const long long tw0 = clock64();
+#endif
+				forEachGroupFragment<true>(p, s, scratch, planes, band_cap, bin_x, bin_y, p0, p1,
+										   [&](int tp, const bool* on, const uint32_t* key, const uint32_t* tri) {
+											   const int end = (tp + 1) * rcap;
+											   int pos[4];
+#pragma unroll
+											   for(int u = 0; u < 4; u++)
+												   pos[u] = on[u] && key[u] >= lo_k && key[u] <= hi_k ? atomicAdd(&s.px_wend[tp], 1) : end;
+#pragma unroll
+											   for(int u = 0; u < 4; u++)
+												   if(pos[u] < end) {
+													   s.kv[1][0][pos[u]] = key[u];
+													   s.kv[1][1][pos[u]] = fragPayload(tp, tri[u]);
+												   }
+										   },
+										   cull ? ekeys : nullptr, 0u, 0, cull ? lo_k : 1u, cull ? hi_k : 0u);
+#if LUCID_RASTER_COUNTERS
+				if(lane == 0)
+					rc[16] += clock64() - tw0;
+#endif
+				__syncthreads();
+#if LUCID_RASTER_COUNTERS
+				if(tid == 0)
+					rc[17] += clock64() - tw0;
+#endif
+				if(__syncthreads_or(t < npix && s.px_wend[t] > (t + 1) * rcap)) {
+					RCOUNT(9, tid == 0);
+					return false;
+				}
+				if(t < npix)
+					s.px_rend[t] = s.px_wend[t] - t * rcap;
+				for(int i = tid; i < (npix << nb_log); i += RT)
+					s.hist[i] = 0;
+				__syncthreads();
+				const int sh = shift;
+				for(int tp = warp; tp < npix; tp += NW) {
+					const int beg = tp * rcap, n = s.px_rend[tp];
+					for(int k = lane; k < n; k += 32)
+						atomicAdd(&s.hist[histIdx(tp, int((s.kv[1][0][beg + k] - lo_k) >> sh), nb_log)], 1u);
+				}
+				__syncthreads();
+				if(t < npix && s.px_state[t] != 1) {
+					s.px_state[t] = 0;
+					s.px_lo[t] = 0;
+				}
+				__syncthreads();
+				RCOUNT(7, tid == 0);
+				return true;
+			};
+			if(windowed) {
+				direct_src = buildSlabDirect();
+				if(!direct_src)
+					buildSlab(0);
+			}
+			RCOUNT(8, tid == 0 && windowed);
 			RASTER_TIMER(2);
 
 			// C2. windows
 			while(true) {
+#if LUCID_RASTER_COUNTERS
+				if(tid == 0)
+					tc2 = clock64();
+#endif
 				// this round's window of every active pixel and the window's sub-segments that need
 				// sorting: one per bucket of the window (heavy group) or one per pixel (light group).
 				// Positions are relative to the pixel's window start until the block scan places
@@ -1257,13 +1434,20 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 						int lbase = 0;
 						if(lane == 0) {
 							if(add)
-								base = atomicAdd(&s.n_cls, add);
+							{
+								// two 32-bit atomics: classes 0-1 and 2-3 (no field carries across)
+								uint32_t* nc32 = reinterpret_cast<uint32_t*>(&s.n_cls);
+								const uint32_t b0 = atomicAdd(nc32, uint32_t(add)), b1 = atomicAdd(nc32 + 1, uint32_t(add >> 32));
+								base = (unsigned long long)b0 | ((unsigned long long)b1 << 32);
+							}
 							if(mlgA | mlgB)
 								lbase = atomicAdd(&s.n_large, __popc(mlgA) + __popc(mlgB));
 						}
 						base = __shfl_sync(0xffffffffu, base, 0);
 						lbase = __shfl_sync(0xffffffffu, lbase, 0);
 						auto put = [&](int cls, int pos, uint32_t entry) {
+							if(pos >= kList) // lists overflow: the window is radix sorted
+								return;
 							if(cls == 0)
 								s.sub_small[pos] = entry;
 							else if(cls == 1)
@@ -1281,9 +1465,10 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 							if(smB && clsB == k)
 								put(k, bk + __popc(mA[k]) + __popc(mB[k] & lt), segEntry(begB, cB, tpB));
 						}
-						if(lgA)
+						constexpr int kLarge = kGroupCap / 17 + 1;
+						if(lgA && lbase + __popc(mlgA & lt) < kLarge)
 							s.sub_large[lbase + __popc(mlgA & lt)] = segEntry(begA, cA, tpA);
-						if(lgB)
+						if(lgB && lbase + __popc(mlgA) + __popc(mlgB & lt) < kLarge)
 							s.sub_large[lbase + __popc(mlgA) + __popc(mlgB & lt)] = segEntry(begB, cB, tpB);
 					}
 					return (inA && cA > 256) || (inB && cB > 256);
@@ -1292,59 +1477,140 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 					return addSegments2(in, beg, c, tp, false, 0, 0, 0);
 				};
 				bool big = false;
+#if LUCID_RASTER_COUNTERS
+				const long long tk0 = clock64();
+#endif
 				if(windowed) {
-					// two pixels per warp at a time (A = tp, B = tp + NW), so that their dependent
-					// steps overlap; each walks its buckets 32 at a time
-					for(int tp = warp; tp < npix; tp += 2 * NW) {
-						const int tpA = tp, tpB = tp + NW;
-						bool doneA = s.px_state[tpA] != 0, doneB = tpB >= npix || s.px_state[tpB] != 0;
-						int accA = 0, cutA = nbuckets - 1, c0A = doneA ? 0 : s.px_lo[tpA];
-						int accB = 0, cutB = nbuckets - 1, c0B = doneB ? 0 : s.px_lo[tpB];
-						const bool actA = !doneA, actB = !doneB;
-						while(!(doneA && doneB)) {
-							const int bkA = c0A + lane, bkB = c0B + lane;
-							const bool okA = !doneA && bkA < nbuckets, okB = !doneB && bkB < nbuckets;
-							const int vA = okA ? int(s.hist[histIdx(tpA, bkA, nb_log)]) : 0;
-							const int vB = okB ? int(s.hist[histIdx(tpB, bkB, nb_log)]) : 0;
-							const int inclA = warpInclusiveScan(vA), inclB = warpInclusiveScan(vB);
-							const uint32_t hitA = __ballot_sync(0xffffffffu, okA && accA + inclA >= kWindow);
-							const uint32_t hitB = __ballot_sync(0xffffffffu, okB && accB + inclB >= kWindow);
-							const int lastA = hitA ? __ffs(hitA) - 1 : 31, lastB = hitB ? __ffs(hitB) - 1 : 31;
-							const bool inA = okA && lane <= lastA, inB = okB && lane <= lastB;
-							const int relA = accA + inclA - vA, relB = accB + inclB - vB;
-							if(inA)
-								s.hist[histIdx(tpA, bkA, nb_log)] = uint32_t(relA);
-							if(inB)
-								s.hist[histIdx(tpB, bkB, nb_log)] = uint32_t(relB);
-							big |= addSegments2(inA, relA, vA, tpA, inB, relB, vB, tpB);
-							const int stA = __shfl_sync(0xffffffffu, inclA, lastA), stB = __shfl_sync(0xffffffffu, inclB, lastB);
-							if(!doneA) {
-								accA += stA;
-								if(hitA)
-									cutA = c0A + lastA, doneA = true;
-								else if((c0A += 32) >= nbuckets)
-									doneA = true;
+					// one warp step per pixel: lane l sums its 2^g buckets from the pixel's first
+					// unprocessed one, a warp scan finds the lane holding the cut, and the lane's
+					// running sum the cut bucket. Two pixels per warp at a time; the sub-segments
+					// of both take their list slots with one packed warp scan and one atomic.
+					constexpr int kList = kGroupCap / 2;
+					const int g = nb_log - 5, G = 1 << g;
+					for(int tp0 = warp; tp0 < npix; tp0 += 2 * NW) {
+						int tpq[2] = {tp0, tp0 + NW};
+						bool act[2];
+						int lsum[2], cntq[2][4], lo[2];
+#pragma unroll
+						for(int q = 0; q < 2; q++) {
+							act[q] = tpq[q] < npix && s.px_state[tpq[q]] == 0;
+							lo[q] = act[q] ? s.px_lo[tpq[q]] : nbuckets;
+							lsum[q] = 0;
+#pragma unroll
+							for(int k = 0; k < 4; k++) {
+								const int bk = (lane << g) + k;
+								const int v = (k < G && act[q] && bk >= lo[q]) ? int(s.hist[histIdx(tpq[q], bk, nb_log)]) : 0;
+								cntq[q][k] = v;
+								lsum[q] += v;
 							}
-							if(!doneB) {
-								accB += stB;
-								if(hitB)
-									cutB = c0B + lastB, doneB = true;
-								else if((c0B += 32) >= nbuckets)
-									doneB = true;
+						}
+						int incl[2], excl[2], cutq[2], accq[2];
+#pragma unroll
+						for(int q = 0; q < 2; q++) {
+							incl[q] = warpInclusiveScan(lsum[q]);
+							excl[q] = incl[q] - lsum[q];
+						}
+						// per lane: included buckets (k <= lastk) and the packed class counts
+						unsigned long long ccount = 0ull;
+						int lcount = 0, lastk[2];
+#pragma unroll
+						for(int q = 0; q < 2; q++) {
+							const uint32_t hit = __ballot_sync(0xffffffffu, act[q] && incl[q] >= kWindow);
+							const int cl = hit ? __ffs(hit) - 1 : 32;
+							int myk = G - 1, run = excl[q];
+							if(lane == cl) {
+								myk = -1;
+#pragma unroll
+								for(int k = 0; k < 4; k++) {
+									if(k < G && myk < 0) {
+										run += cntq[q][k];
+										if(run >= kWindow)
+											myk = k;
+									}
+								}
+							}
+							lastk[q] = !act[q] || lane > cl ? -1 : lane < cl ? G - 1 : myk;
+							const int kc = __shfl_sync(0xffffffffu, myk, cl & 31);
+							cutq[q] = hit ? (cl << g) + kc : nbuckets - 1;
+							// the window's fragments: everything up to the cut
+							const int upto = hit ? __shfl_sync(0xffffffffu, run, cl & 31) : __shfl_sync(0xffffffffu, incl[q], 31);
+							accq[q] = upto;
+#pragma unroll
+							for(int k = 0; k < 4; k++) {
+								const int c = cntq[q][k];
+								if(k <= lastk[q] && c >= 2) {
+									if(c <= 16)
+										ccount += 1ull << (16 * (c <= 2 ? 0 : c <= 4 ? 1 : c <= 8 ? 2 : 3));
+									else if(c <= 256)
+										lcount++;
+									else
+										big = true;
+								}
+							}
+						}
+						const unsigned long long cincl = warpInclusiveScan(ccount);
+						const int lincl = warpInclusiveScan(lcount);
+						unsigned long long cbase = 0ull;
+						int lbase = 0;
+						if(lane == 31) {
+							if(cincl)
+							{
+								uint32_t* nc32 = reinterpret_cast<uint32_t*>(&s.n_cls);
+								const uint32_t b0 = atomicAdd(nc32, uint32_t(cincl)), b1 = atomicAdd(nc32 + 1, uint32_t(cincl >> 32));
+								cbase = (unsigned long long)b0 | ((unsigned long long)b1 << 32);
+							}
+							if(lincl)
+								lbase = atomicAdd(&s.n_large, lincl);
+						}
+						cbase = __shfl_sync(0xffffffffu, cbase, 31);
+						lbase = __shfl_sync(0xffffffffu, lbase, 31);
+						unsigned long long cpos = cbase + cincl - ccount; // this lane's first slot per class
+						int lpos = lbase + lincl - lcount;
+#pragma unroll
+						for(int q = 0; q < 2; q++) {
+							int rel = excl[q];
+#pragma unroll
+							for(int k = 0; k < 4; k++) {
+								const int c = cntq[q][k];
+								if(k <= lastk[q]) {
+									const int bk = (lane << g) + k;
+									if(bk >= lo[q]) {
+										s.hist[histIdx(tpq[q], bk, nb_log)] = uint32_t(rel);
+										if(c >= 2 && c <= 16) {
+											const int cls = c <= 2 ? 0 : c <= 4 ? 1 : c <= 8 ? 2 : 3;
+											const int pos = int((cpos >> (16 * cls)) & 0xffffull);
+											cpos += 1ull << (16 * cls);
+											const uint32_t entry = segEntry(rel, c, tpq[q]);
+											if(pos >= kList) // lists overflow: the window is radix sorted
+												;
+											else if(cls == 0)
+												s.sub_small[pos] = entry;
+											else if(cls == 1)
+												s.radix[pos] = entry;
+											else if(cls == 2)
+												s.sub_small[kList - 1 - pos] = entry;
+											else
+												s.radix[kList - 1 - pos] = entry;
+										} else if(c > 16 && c <= 256) {
+											if(lpos < kGroupCap / 17 + 1)
+												s.sub_large[lpos] = segEntry(rel, c, tpq[q]);
+											lpos++;
+										}
+									}
+								}
+								rel += c;
 							}
 						}
 						if(lane == 0) {
-							if(actA) {
-								s.px_cut[tpA] = cutA;
-								s.px_wcnt[tpA] = accA;
-								if(accA == 0) // nothing left in this slab: wait for the next one, or done
-									s.px_state[tpA] = (s.px_done[tpA] < s.pix_count[p0 + tpA] && s.slab_hi < s.kmax) ? 2 : 1;
-							}
-							if(actB) {
-								s.px_cut[tpB] = cutB;
-								s.px_wcnt[tpB] = accB;
-								if(accB == 0)
-									s.px_state[tpB] = (s.px_done[tpB] < s.pix_count[p0 + tpB] && s.slab_hi < s.kmax) ? 2 : 1;
+#pragma unroll
+							for(int q = 0; q < 2; q++) {
+								if(!act[q])
+									continue;
+								const int tp = tpq[q];
+								s.px_cut[tp] = cutq[q];
+								s.px_wcnt[tp] = accq[q];
+								if(accq[q] == 0)
+									s.px_state[tp] = (s.px_done[tp] < s.pix_count[p0 + tp] && s.slab_hi < s.kmax) ? 2 : 1;
 							}
 						}
 					}
@@ -1357,7 +1623,17 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 					}
 					big = addSegments(in, 0, c, t);
 				}
+#if LUCID_RASTER_COUNTERS
+				if(tid == 0)
+					rc[15] += clock64() - tc2;
+				if(lane == 0)
+					rc[18] += clock64() - tk0;
+#endif
 				__syncthreads();
+#if LUCID_RASTER_COUNTERS
+				if(tid == 0)
+					rc[19] += clock64() - tk0;
+#endif
 				int wcount = t < npix && s.px_state[t] == 0 ? s.px_wcnt[t] : 0;
 				int total;
 				int wbase = blockExclusiveScan(wcount, s.scan_tmp, &total);
@@ -1419,23 +1695,69 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 							s.px_cut[tp] = -1, s.px_wcnt[tp] = 0;
 					}
 				}
+				if(tid == 0) {
+					// sub-segment lists longer than their arrays (a window of many equal-depth
+					// runs) send the window to the radix sort
+					const unsigned long long nc = s.n_cls;
+					constexpr int kList = kGroupCap / 2;
+					const int n0 = int(nc & 0xffffu), n1 = int((nc >> 16) & 0xffffu);
+					const int n2 = int((nc >> 32) & 0xffffu), n3 = int(nc >> 48);
+					if(n0 + n2 > kList || n1 + n3 > kList || s.n_large > kGroupCap / 17 + 1)
+						big = true;
+				}
 				const bool any_big = __syncthreads_or(big);
 				if(!__syncthreads_or(wcount > 0)) {
 					if(windowed && __syncthreads_or(t < npix && s.px_state[t] == 2)) {
+						direct_src = false;
 						buildSlab(s.slab_next); // a waiting pixel implies slab_hi < kmax
 						continue;
 					}
 					break;
 				}
 				const int n = total;
+#if LUCID_RASTER_COUNTERS
+				if(tid == 0) {
+					const long long now = clock64();
+					rc[12] += now - tc2;
+					tc2 = now;
+				}
+				RCOUNT(11, tid == 0);
+				unsigned long long* ec6 = &rc[6];
+#else
+				unsigned long long* ec6 = nullptr;
+#endif
 
 				// C3. window fragments into their sub-segments. A lane always visits the same pixel,
 				// so its window (as a key range), cursor base and end are read once.
+				if(windowed && direct_src) {
+					// the first window of a direct slab: from the pixels' regions
+					direct_src = false;
+					for(int tp = warp; tp < npix; tp += NW) {
+						const int cut = s.px_cut[tp];
+						if(cut < 0)
+							continue;
+						const uint32_t w_lo = uint32_t((unsigned long long)slab_lo + ((unsigned long long)s.px_lo[tp] << shift));
+						const unsigned long long z = (unsigned long long)slab_lo + ((unsigned long long)(cut + 1) << shift) - 1ull;
+						const uint32_t w_hi = uint32_t(z < (unsigned long long)slab_hi ? z : (unsigned long long)slab_hi);
+						const int base = s.px_wbase[tp], end = base + s.px_wcnt[tp];
+						const int beg = tp * rcap, n = s.px_rend[tp];
+						for(int k = lane; k < n; k += 32) {
+							const uint32_t key = s.kv[1][0][beg + k];
+							if(key < w_lo || key > w_hi)
+								continue;
+							const int pos = base + int(atomicAdd(&s.hist[histIdx(tp, int((key - slab_lo) >> shift), nb_log)], 1u));
+							if(pos < end) {
+								s.kv[0][0][pos] = key;
+								s.kv[0][1][pos] = s.kv[1][1][beg + k];
+							}
+						}
+					}
+				} else
 				if(windowed) {
 					int c_tp = -1, c_base = 0, c_end = 0;
 					uint32_t c_klo = 1u, c_khi = 0u;
-					forEachGroupFragment(p, s, scratch, planes, band_cap, bin_x, bin_y, p0, p1,
-										 [&](int tp, uint32_t key, uint32_t tri) {
+					forEachGroupFragment<true>(p, s, scratch, planes, band_cap, bin_x, bin_y, p0, p1,
+										 [&](int tp, const bool* on, const uint32_t* key, const uint32_t* tri) {
 											 if(tp != c_tp) {
 												 c_tp = tp;
 												 const int cut = s.px_cut[tp];
@@ -1451,16 +1773,25 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 												 c_base = s.px_wbase[tp];
 												 c_end = c_base + s.px_wcnt[tp];
 											 }
-											 if(key < c_klo || key > c_khi)
-												 return;
-											 const int bk = int((key - slab_lo) >> shift);
-											 const int pos = c_base + int(atomicAdd(&s.hist[histIdx(tp, bk, nb_log)], 1u));
-											 if(pos < c_end) {
-												 s.kv[0][0][pos] = key;
-												 s.kv[0][1][pos] = fragPayload(tp, tri);
+											 bool w[4];
+											 int pos[4];
+#pragma unroll
+											 for(int u = 0; u < 4; u++) {
+												 w[u] = on[u] && key[u] >= c_klo && key[u] <= c_khi;
+												 RCOUNT(3, on[u]);
+												 RCOUNT(4, w[u]);
 											 }
+#pragma unroll
+											 for(int u = 0; u < 4; u++)
+												 pos[u] = w[u] ? c_base + int(atomicAdd(&s.hist[histIdx(tp, int((key[u] - slab_lo) >> shift), nb_log)], 1u)) : c_end;
+#pragma unroll
+											 for(int u = 0; u < 4; u++)
+												 if(pos[u] < c_end) {
+													 s.kv[0][0][pos[u]] = key[u];
+													 s.kv[0][1][pos[u]] = fragPayload(tp, tri[u]);
+												 }
 										 },
-										 ekeys, slab_lo, shift);
+										 ekeys, slab_lo, shift, 1u, 0u, ec6);
 				} else {
 					forEachGroupFragment(p, s, scratch, planes, band_cap, bin_x, bin_y, p0, p1,
 										 [&](int tp, uint32_t key, uint32_t tri) {
@@ -1485,6 +1816,10 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 					s.px_wend[t] = want;
 				}
 				__syncthreads();
+#if LUCID_RASTER_COUNTERS
+				if(tid == 0)
+					rc[13] += clock64() - tc2;
+#endif
 				RASTER_TIMER(3);
 
 				// C4. sort every sub-segment by key: small ones by one thread, larger ones (<= 256)
@@ -1610,22 +1945,38 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 						// slot / batch by multiply and shift (exact for odd batch in [15, 255] and
 						// slot < 4096)
 						const uint32_t bmul = (1u << 20) / uint32_t(batch) + 1u;
-#pragma unroll 2
-						for(int slot = tid; slot < npix * batch; slot += RT) {
-							int tp = int((uint32_t(slot) * bmul) >> 20), j = slot - tp * batch;
-							int f = s.px_bcur[tp] + j;
-							if(f < s.px_wend[tp] && s.px_state[tp] == 0) {
-								uint32_t v = V[f];
-								uint32_t tri = payloadTri(v);
-								int pl = p0 + int(v & 0xffu);
-								float4 c = shadeFragment(p, tri, keyToDepth(K[f]), bin_x + (pl & 31),
-														 bin_y + (pl >> 5));
-								// the forward blend needs only the premultiplied colour and 1 - alpha:
-								// computed here in parallel, the same FP32 operations as in the blend
-								if constexpr(MODE == kRasterForward)
-									c = make_float4(c.x * c.w, c.y * c.w, c.z * c.w, 1.0f - c.w);
-								stage[slot] = c;
+						// two slots per thread per step: both fragments' payloads and keys are read
+						// before either is shaded, so that their record loads and FP32 chains overlap
+						const int nslots = npix * batch;
+						for(int slot0 = tid; slot0 < nslots; slot0 += 2 * RT) {
+							int fq[2], tq[2];
+							bool okq[2];
+							uint32_t vq[2], kq[2];
+#pragma unroll
+							for(int q = 0; q < 2; q++) {
+								const int slot = slot0 + q * RT;
+								tq[q] = int((uint32_t(slot) * bmul) >> 20);
+								const int tpc = min(tq[q], npix - 1);
+								fq[q] = s.px_bcur[tpc] + (slot - tq[q] * batch);
+								okq[q] = slot < nslots && fq[q] < s.px_wend[tpc] && s.px_state[tpc] == 0;
+								vq[q] = okq[q] ? V[fq[q]] : 0u;
+								kq[q] = okq[q] ? K[fq[q]] : 0u;
 							}
+							float4 cq[2];
+#pragma unroll
+							for(int q = 0; q < 2; q++) {
+								const int pl = p0 + int(vq[q] & 0xffu);
+								cq[q] = okq[q] ? shadeFragment(p, payloadTri(vq[q]), keyToDepth(kq[q]), bin_x + (pl & 31), bin_y + (pl >> 5))
+											   : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+								if constexpr(MODE == kRasterForward)
+									cq[q] = make_float4(cq[q].x * cq[q].w, cq[q].y * cq[q].w, cq[q].z * cq[q].w, 1.0f - cq[q].w);
+							}
+#pragma unroll
+							for(int q = 0; q < 2; q++)
+								if(okq[q]) {
+									RCOUNT(10, 1);
+									stage[slot0 + q * RT] = cq[q];
+								}
 						}
 					}
 					__syncthreads();
@@ -1846,6 +2197,17 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 	if(timers && tid == 0)
 		for(int i = 0; i < 8; i++)
 			atomicAdd(&timer_info->raster_timers[i], uint32_t(tacc[i] >> 8));
+#if LUCID_RASTER_COUNTERS
+	if(timers)
+		for(int i = 0; i < 24; i++) {
+			unsigned long long v = rc[i];
+#pragma unroll
+			for(int o = 16; o > 0; o >>= 1)
+				v += __shfl_xor_sync(0xffffffffu, v, o);
+			if(lane == 0 && v)
+				atomicAdd(reinterpret_cast<unsigned long long*>(timer_info->temp) + i, v);
+		}
+#endif
 #undef RASTER_TIMER
 }
 
