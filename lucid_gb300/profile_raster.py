@@ -7,8 +7,9 @@ The frame is rendered with LUCID_OPT_TIMERS by the counters build of the library
 library is not loaded). Phase times are SM time per SM (clock64 deltas of thread 0 between the
 raster kernel's CTA barriers, summed over the persistent CTAs and divided by the SM count)
 at the SM clock given by --mhz; the counters are the ones listed at the top of
-csrc/lucid_raster.cu. ms_frame is a frame of the same workload timed with CUDA events without
-timers.
+csrc/lucid_raster.cu. ms_frame is a frame of the same workload by the counters build, timed
+with CUDA events without timers (the counters cost a few spilled registers: it is slower than
+the product library's frame).
 """
 from __future__ import annotations
 
