@@ -220,7 +220,10 @@ typedef struct lucid_info {
 
 typedef struct lucid_options {
 	uint32_t flags;            /* LUCID_OPT_*                                                  */
-	int32_t bin_size;          /* must be 32 (src/lucid_renderer.cpp:190)                      */
+	int32_t bin_size;          /* 32 or 64 pixels (src/lucid_renderer.cpp:190: m_bin_size, whose
+	                            * 64 option is commented out in the reference); 64-pixel bins
+	                            * are rastered as four 32x32 tiles. The reference-order mode and
+	                            * lucid_raster_dump_bins need 32. Buffers are sized for 32.  */
 	int32_t max_input_quads;   /* capacity of the per-input-quad classification buffer        */
 	int32_t max_visible_quads; /* MAX_VISIBLE_QUADS (definitions.glsl:54)                      */
 	int32_t max_instances;     /* src/lucid_renderer.h:28 (64K)                                */
@@ -446,18 +449,18 @@ typedef struct lucid_tuning {
 	float frame_ms;             /* median frame time of the winner                               */
 	float default_ms;           /* median frame time of the renderer's options before tuning     */
 	int32_t light_max_pixel;    /* deepest pixel of a bin rastered one warp per row (-1: none)  */
-	int32_t reserved[1];
+	int32_t bin_size;           /* bins of 32 or 64 pixels                                       */
 } lucid_tuning;
 
 /* Autotuner (no reference counterpart): times lucid_render of `inputs` into scratch_rgba
  * (device, width*height*4 floats) under candidate configurations, by coordinate descent over
- * the blend strategy (raster-pass blend or LUCID_OPT_PIXEL_BLEND), the LOW/HIGH threshold
- * (256, 1024, 4096), the binning CTAs (1 or 2 per SM, within options.binning_ctas) and the
- * per-bin raster path (options.light_max_pixel: -1, 32, 64, 128, 256; bins up to that depth are
- * rastered one warp per row, deeper ones by CTA-wide depth windows); CUDA events on `stream`,
- * median of 3 frames after one warm-up frame each. The winner is stored in the renderer's
- * options and returned in *out (may be NULL). Synchronous. Bin size is fixed at 32 (the
- * reference's only enabled size); raster CTAs are one per SM (shared memory). */
+ * the bin size (32 or 64 pixels; not in the reference-order mode), the blend strategy
+ * (raster-pass blend or LUCID_OPT_PIXEL_BLEND), the LOW/HIGH threshold (256, 1024, 4096), the
+ * binning CTAs (1 or 2 per SM, within options.binning_ctas) and the per-bin raster path
+ * (options.light_max_pixel: -1, 32, 64, 128, 256; bins up to that depth are rastered one warp
+ * per row, deeper ones by CTA-wide depth windows); CUDA events on `stream`, median of 3 frames
+ * after one warm-up frame each. The winner is stored in the renderer's options and returned in
+ * *out (may be NULL). Synchronous. Raster CTAs are one per SM (shared memory). */
 lucid_status lucid_autotune(lucid_renderer* renderer, const lucid_frame_inputs* inputs,
 							float* scratch_rgba, lucid_tuning* out, void* stream);
 

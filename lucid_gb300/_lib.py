@@ -92,7 +92,7 @@ class CameraC(ctypes.Structure):
 class Tuning(ctypes.Structure):
     _fields_ = [("pixel_blend", c_uint32), ("low_high_threshold", c_int32), ("binning_ctas", c_int32),
                 ("num_candidates", c_int32), ("frame_ms", ctypes.c_float), ("default_ms", ctypes.c_float),
-                ("light_max_pixel", c_int32), ("reserved", c_int32 * 1)]
+                ("light_max_pixel", c_int32), ("bin_size", c_int32)]
 
 
 class ViewC(ctypes.Structure):

@@ -33,16 +33,17 @@ struct BinScan {
 	float mn[3], mx[3], step[3];
 };
 
-// scanline.glsl:28-52 (loadScanlineParamsBin)
+// scanline.glsl:28-52 (loadScanlineParamsBin) for bins of 1 << bsh pixels (BIN_SIZE, BIN_SHIFT)
 __device__ __forceinline__ BinScan loadScanlineParamsBin(uint4 r0, uint4 r1, int& min_by,
-														 int& max_by) {
+														 int& max_by, int bsh) {
 	BinScan s;
 	float scan[3] = {bitsf(r0.x), bitsf(r0.y), bitsf(r0.z)};
 	s.step[0] = bitsf(r1.x), s.step[1] = bitsf(r1.y), s.step[2] = bitsf(r1.z);
-	min_by = int(r0.w & 0xffffu) >> kBinShift;
-	max_by = int(r0.w >> 16) >> kBinShift;
-	const float offset = float(kBinSize) - 0.989f;
-	const float start_x = 0.99f, start_y = float(min_by * kBinSize) - 0.01f;
+	min_by = int(r0.w & 0xffffu) >> bsh;
+	max_by = int(r0.w >> 16) >> bsh;
+	const float bin_size = float(1 << bsh);
+	const float offset = bin_size - 0.989f;
+	const float start_x = 0.99f, start_y = float(min_by << bsh) - 0.01f;
 #pragma unroll
 	for(int i = 0; i < 3; i++) {
 		bool xneg = (r1.w >> i) & 1u, yneg = (r1.w >> (3 + i)) & 1u;
@@ -50,20 +51,20 @@ __device__ __forceinline__ BinScan loadScanlineParamsBin(uint4 r0, uint4 r1, int
 		scan[i] = scan[i] + (s.step[i] * (yoff + start_y) - (xoff + start_x));
 		s.mn[i] = xneg ? -INFINITY : scan[i];
 		s.mx[i] = xneg ? scan[i] : INFINITY;
-		s.step[i] = s.step[i] * float(kBinSize);
+		s.step[i] = s.step[i] * bin_size;
 	}
 	return s;
 }
 
 // bin_counter.glsl:53-62 (scanlineStep)
-__device__ __forceinline__ void scanlineStep(BinScan& s, int& bmin, int& bmax) {
+__device__ __forceinline__ void scanlineStep(BinScan& s, int& bmin, int& bmax, int bsh) {
 	float xmin = fmaxf(fmaxf(s.mn[0], s.mn[1]), s.mn[2]);
 	float xmax = fminf(fminf(s.mx[0], s.mx[1]), s.mx[2]);
 #pragma unroll
 	for(int i = 0; i < 3; i++)
 		s.mn[i] += s.step[i], s.mx[i] += s.step[i];
-	bmin = f2i(xmin + 1.0f) >> kBinShift;
-	bmax = f2i(xmax) >> kBinShift;
+	bmin = f2i(xmin + 1.0f) >> bsh;
+	bmax = f2i(xmax) >> bsh;
 }
 
 __device__ __forceinline__ void ctaRange(int n, int cta, int ncta, int& beg, int& end) {
@@ -91,6 +92,14 @@ __device__ __forceinline__ uint32_t warpBinSlot(int* s_bins, int key) {
 		base = atomicAdd(&s_bins[key], __popc(peers));
 	base = __shfl_sync(0xffffffffu, base, leader);
 	return uint32_t(base + __popc(peers & laneMaskLt()));
+}
+
+// The bins of an encoded AABB (setup encodes it in 32-pixel bins, 7 bits per coordinate) in the
+// frame's bins of 1 << bin_shift pixels; an empty AABB stays empty.
+__device__ __forceinline__ void decodeBinAABB(const FrameParams& p, uint32_t enc, int& x0, int& y0, int& x1, int& y1) {
+	decodeAABB28(enc, x0, y0, x1, y1);
+	const int sh = p.bin_shift - kBinShift;
+	x0 >>= sh, y0 >>= sh, x1 >>= sh, y1 >>= sh;
 }
 
 // Bin j (0..3) of a small quad's bin AABB (at most 4 bins, bin_counter.glsl:64-80), -1 if none.
@@ -133,7 +142,7 @@ template <class Src> __global__ void __launch_bounds__(kBinningThreads, 1) binCo
 		const int k = base + lane;
 		int x0 = 0, y0 = 0, x1 = -1, y1 = -1;
 		if(k < send)
-			decodeAABB28(p.quad_aabbs[k], x0, y0, x1, y1);
+			decodeBinAABB(p, p.quad_aabbs[k], x0, y0, x1, y1);
 		const int nb = __reduce_max_sync(0xffffffffu, (x1 - x0 + 1) * (y1 - y0 + 1));
 		for(int j = 0; j < nb; j++)
 			warpAddBin(s_bins, k < send ? smallQuadBin(x0, y0, x1, y1, bcx, j) : -1, 1);
@@ -160,12 +169,13 @@ template <class Src> __global__ void __launch_bounds__(kBinningThreads, 1) binCo
 		if(!largeTri(p, lbeg, it, tri, enc))
 			continue;
 		int x0, y0, x1, y1;
-		decodeAABB28(enc, x0, y0, x1, y1);
+		decodeBinAABB(p, enc, x0, y0, x1, y1);
 		int bsy, bey;
-		BinScan sc = loadScanlineParamsBin(p.tri_scan[size_t(tri) * 2], p.tri_scan[size_t(tri) * 2 + 1], bsy, bey);
+		BinScan sc = loadScanlineParamsBin(p.tri_scan[size_t(tri) * 2], p.tri_scan[size_t(tri) * 2 + 1], bsy, bey,
+										   p.bin_shift);
 		for(int by = bsy; by <= bey; by++) {
 			int bmin, bmax;
-			scanlineStep(sc, bmin, bmax);
+			scanlineStep(sc, bmin, bmax, p.bin_shift);
 			bmin = max(bmin, x0), bmax = min(bmax, x1);
 			if(bmax >= bmin) {
 				atomicAdd(&s_bins[bmin + by * bcx], 1);
@@ -324,7 +334,7 @@ template <class Src> __global__ void __launch_bounds__(kBinningThreads, 1) binDi
 		if(k < send) {
 			const uint32_t enc = p.quad_aabbs[k];
 			entry = uint32_t(k) | (enc & 0xf0000000u);
-			decodeAABB28(enc, x0, y0, x1, y1);
+			decodeBinAABB(p, enc, x0, y0, x1, y1);
 		}
 		const int nb = __reduce_max_sync(0xffffffffu, (x1 - x0 + 1) * (y1 - y0 + 1));
 		for(int j = 0; j < nb; j++) {
@@ -351,12 +361,13 @@ template <class Src> __global__ void __launch_bounds__(kBinningThreads, 1) binDi
 		if(!largeTri(p, lbeg, it, tri, enc))
 			continue;
 		int x0, y0, x1, y1;
-		decodeAABB28(enc, x0, y0, x1, y1);
+		decodeBinAABB(p, enc, x0, y0, x1, y1);
 		int bsy, bey;
-		BinScan sc = loadScanlineParamsBin(p.tri_scan[size_t(tri) * 2], p.tri_scan[size_t(tri) * 2 + 1], bsy, bey);
+		BinScan sc = loadScanlineParamsBin(p.tri_scan[size_t(tri) * 2], p.tri_scan[size_t(tri) * 2 + 1], bsy, bey,
+										   p.bin_shift);
 		for(int by = bsy; by <= bey; by++) {
 			int bmin, bmax;
-			scanlineStep(sc, bmin, bmax);
+			scanlineStep(sc, bmin, bmax, p.bin_shift);
 			bmin = max(bmin, x0), bmax = min(bmax, x1);
 			for(int bx = bmin; bx <= bmax; bx++) {
 				uint32_t slot = uint32_t(atomicAdd(&s_bins[by * bcx + bx], 1));

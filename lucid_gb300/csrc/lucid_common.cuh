@@ -47,6 +47,9 @@ struct FrameParams {
 	// ---- dimensions & limits ----
 	int width, height;
 	int bin_count_x, bin_count_y, bin_count;
+	// bins are (1 << bin_shift) pixels square: 32 (5) or 64 (6). Setup's bin AABBs and the
+	// raster tiles stay 32x32; a 64-pixel bin is rastered as its four 32x32 tiles.
+	int bin_shift;
 	int max_visible_quads;
 	int max_bin_refs;
 	int band_capacity;

@@ -121,6 +121,8 @@ struct lucid_renderer {
 
 	struct BatchPlan* batch = nullptr; // lucid_render_batch state (plan, buffers, graph)
 
+	// bin_count_x / _y / bin_count are the 32-pixel grid the buffers are sized for; a frame
+	// with 64-pixel bins (options.bin_size) uses the smaller grid of frameBins()
 	size_t infoBytes() const { return sizeof(lucid_info) + size_t(10) * bin_count * 4; }
 	lucid_info* info() const { return reinterpret_cast<lucid_info*>(info_block); }
 	uint32_t* counts() const { return reinterpret_cast<uint32_t*>(info_block + sizeof(lucid_info)); }
@@ -190,9 +192,24 @@ int lightMaxPixel(const lucid_options* o) {
 	return o->light_max_pixel == 0 ? 64 : (o->light_max_pixel < 0 ? -1 : o->light_max_pixel);
 }
 int lightMaxPixel(const lucid_renderer* r) { return lightMaxPixel(&r->opts); }
+// bins of options.bin_size pixels (32 or 64): log2 of the size, the grid of a viewport, and the
+// number of bins of the renderer's current frames
+int binShift(const lucid_options& o) { return o.bin_size == 64 ? 6 : kBinShift; }
+void binGrid(int w, int h, int bsh, int& bcx, int& bcy) {
+	const int bs = 1 << bsh;
+	bcx = (w + bs - 1) / bs, bcy = (h + bs - 1) / bs;
+}
+int frameBins(const lucid_renderer* r) {
+	int bcx, bcy;
+	binGrid(r->width, r->height, binShift(r->opts), bcx, bcy);
+	return bcx * bcy;
+}
 
 FrameParams makeParams(lucid_renderer* r, const lucid_frame_inputs* in, float* out) {
 	FrameParams p{};
+	p.bin_shift = binShift(r->opts);
+	binGrid(r->width, r->height, p.bin_shift, p.bin_count_x, p.bin_count_y);
+	p.bin_count = p.bin_count_x * p.bin_count_y;
 	p.positions = in->positions;
 	p.colors = in->colors;
 	p.color_format = in->color_format;
@@ -207,7 +224,6 @@ FrameParams makeParams(lucid_renderer* r, const lucid_frame_inputs* in, float* o
 	p.out_rgba = out;
 	p.cfg = *in->config;
 	p.width = r->width, p.height = r->height;
-	p.bin_count_x = r->bin_count_x, p.bin_count_y = r->bin_count_y, p.bin_count = r->bin_count;
 	p.max_visible_quads = r->opts.max_visible_quads;
 	p.max_bin_refs = r->opts.max_bin_refs;
 	p.band_capacity = r->opts.band_capacity;
@@ -412,8 +428,8 @@ extern "C" lucid_status lucid_create(const lucid_options* options, int32_t width
 		o = *options;
 	else
 		lucid_default_options(&o);
-	if(o.bin_size != 32)
-		return fail(LUCID_NOT_SUPPORTED, "only 32x32 bins are supported");
+	if(o.bin_size != 32 && o.bin_size != 64)
+		return fail(LUCID_NOT_SUPPORTED, "bins must be 32x32 or 64x64 pixels");
 	if(width <= 0 || height <= 0 || width > 4096 || height > 4096)
 		return fail(LUCID_INVALID_ARG, "viewport must be within 1..4096 pixels per axis");
 	if(o.max_visible_quads <= 0 || o.max_visible_quads > (1 << 23) || o.max_input_quads <= 0 ||
@@ -629,6 +645,8 @@ static lucid_status rasterImpl(lucid_renderer* r, const lucid_frame_inputs* in, 
 	if(r->opts.flags & LUCID_OPT_REFERENCE_ORDER) {
 		if(r->opts.flags & LUCID_OPT_ALPHA_THRESHOLD)
 			return fail(LUCID_NOT_SUPPORTED, "the reference-order mode has no alpha-threshold variant");
+		if(r->opts.bin_size != 32)
+			return fail(LUCID_NOT_SUPPORTED, "the reference-order mode needs 32x32 bins");
 		if((st = resetRasterCounters(r, s)) != LUCID_OK)
 			return st;
 		LUCID_CUDA_TRY(cudaMemsetAsync(&r->info()->stats[2], 0, 4, s));
@@ -670,7 +688,7 @@ extern "C" lucid_status lucid_get_info(lucid_renderer* r, lucid_info* out, uint3
 	LUCID_CUDA_TRY(cudaStreamSynchronize(s));
 	LUCID_CUDA_TRY(cudaMemcpy(out, r->info_block, sizeof(lucid_info), cudaMemcpyDeviceToHost));
 	if(bin_counters)
-		LUCID_CUDA_TRY(cudaMemcpy(bin_counters, r->counts(), size_t(10) * r->bin_count * 4,
+		LUCID_CUDA_TRY(cudaMemcpy(bin_counters, r->counts(), size_t(10) * frameBins(r) * 4,
 								  cudaMemcpyDeviceToHost));
 	return LUCID_OK;
 }
@@ -722,6 +740,8 @@ static lucid_status rasterDump(lucid_renderer* r, const lucid_frame_inputs* in, 
 	std::vector<int> slots;
 	if(bins && (r->opts.flags & LUCID_OPT_REFERENCE_ORDER))
 		return fail(LUCID_NOT_SUPPORTED, "lucid_raster_dump_bins: not in the reference-order mode");
+	if(bins && r->opts.bin_size != 32)
+		return fail(LUCID_NOT_SUPPORTED, "lucid_raster_dump_bins: needs 32x32 bins");
 	if(bins) {
 		if(num_bins <= 0 || num_bins > r->bin_count)
 			return fail(LUCID_INVALID_ARG, "lucid_raster_dump_bins: num_bins out of range");
@@ -1054,10 +1074,11 @@ int viewBinningCtas(const lucid_renderer* r, int nq) {
 	return std::max(1, std::min(r->opts.binning_ctas, (nq + 2047) / 2048));
 }
 
-std::vector<int64_t> batchKey(const lucid_view* views, int n) {
+std::vector<int64_t> batchKey(const lucid_renderer* r, const lucid_view* views, int n) {
 	std::vector<int64_t> key;
-	key.reserve(1 + 4 * size_t(n));
+	key.reserve(2 + 4 * size_t(n));
 	key.push_back(n);
+	key.push_back(r->opts.bin_size);
 	for(int v = 0; v < n; v++) {
 		key.push_back(views[v].width);
 		key.push_back(views[v].height);
@@ -1090,8 +1111,8 @@ void batchParams(lucid_renderer* r, BatchPlan* b, const lucid_view* views, std::
 		p.out_rgba = vw.out_rgba;
 		p.cfg = *in.config;
 		p.width = vw.width, p.height = vw.height;
-		p.bin_count_x = (vw.width + kBinSize - 1) / kBinSize;
-		p.bin_count_y = (vw.height + kBinSize - 1) / kBinSize;
+		p.bin_shift = binShift(r->opts);
+		binGrid(vw.width, vw.height, p.bin_shift, p.bin_count_x, p.bin_count_y);
 		p.bin_count = p.bin_count_x * p.bin_count_y;
 		const int nq = in.num_quads;
 		const int cap = std::max(nq, 1);
@@ -1260,7 +1281,7 @@ extern "C" lucid_status lucid_render_batch(lucid_renderer* r, const lucid_view* 
 										 "call it outside stream capture");
 	r->have_frame = false; // the single-view buffers are reused by the batch
 	r->grad_ready = false;
-	std::vector<int64_t> key = batchKey(views, num_views);
+	std::vector<int64_t> key = batchKey(r, views, num_views);
 	lucid_status st;
 	if(!r->batch || r->batch->key != key) {
 		if((st = buildBatchPlan(r, views, num_views, std::move(key), s)) != LUCID_OK)
@@ -1363,10 +1384,18 @@ extern "C" lucid_status lucid_autotune(lucid_renderer* r, const lucid_frame_inpu
 			r->opts = best;
 			return rs;
 		};
-		// 1. blend strategy
 		lucid_options o = best;
+		// 0. bin size: 32 or 64 pixels (64-pixel bins are rastered as four 32x32 tiles: fewer
+		// bin references and binning atomics, each tile scans its bin's whole lists)
+		if(!(best.flags & LUCID_OPT_REFERENCE_ORDER)) {
+			o.bin_size = best.bin_size == 64 ? 32 : 64;
+			st = tryOpts(o);
+		}
+		// 1. blend strategy
+		o = best;
 		o.flags ^= LUCID_OPT_PIXEL_BLEND;
-		st = tryOpts(o);
+		if(st == LUCID_OK)
+			st = tryOpts(o);
 		// 2. LOW/HIGH threshold (raster work order)
 		for(int th : {256, 1024, 4096}) {
 			if(st != LUCID_OK || th == best.low_high_threshold)
@@ -1406,6 +1435,7 @@ extern "C" lucid_status lucid_autotune(lucid_renderer* r, const lucid_frame_inpu
 		out->low_high_threshold = r->opts.low_high_threshold;
 		out->binning_ctas = r->opts.binning_ctas;
 		out->light_max_pixel = lightMaxPixel(r);
+		out->bin_size = r->opts.bin_size;
 		out->num_candidates = candidates;
 		out->frame_ms = best_ms;
 		out->default_ms = default_ms;

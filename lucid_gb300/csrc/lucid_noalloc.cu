@@ -110,6 +110,7 @@ extern "C" lucid_status lucid_bin_noalloc(const uint32_t* quad_aabbs, const uint
 	FrameParams p{};
 	p.width = width, p.height = height;
 	p.bin_count_x = bcx, p.bin_count_y = bcy, p.bin_count = bcx * bcy;
+	p.bin_shift = kBinShift; // 32x32 bins
 	p.max_visible_quads = max_visible_quads;
 	p.max_bin_refs = max_bin_refs;
 	p.low_high_threshold = low_high_threshold;

@@ -122,6 +122,7 @@ struct RasterSmem {
 	int slab_next;             // index of the next slab
 	int slab_first[kMaxSlabs]; // first estimate bin of every slab (INT_MAX: no such slab)
 	int bin;
+	int tile;        // 32x32 tile of a 64-pixel bin (0..3: x = tile & 1, y = tile >> 1)
 	int group_end;
 	int single_digit;
 	int any_big;
@@ -758,10 +759,13 @@ struct OneViewWork {
 	FrameParams p;
 	__device__ __forceinline__ const FrameParams& first() const { return p; }
 	__device__ __forceinline__ lucid_info* timerInfo() const { return p.info; }
-	// thread 0: next bin of the work list (HIGH, LOW, EMPTY), -1 when done
+	// thread 0: next tile of the work list (the bins HIGH, LOW, EMPTY, each as its tiles: one
+	// for 32-pixel bins, four for 64-pixel bins), bin -1 when done
 	__device__ __forceinline__ void next(RasterSmem& s) const {
-		uint32_t w = atomicAdd(&p.info->raster_work_counter, 1u);
-		s.bin = w < uint32_t(p.bin_count) ? int(p.raster_work[w]) : -1;
+		const int tsh = 2 * (p.bin_shift - kBinShift);
+		const uint32_t w = atomicAdd(&p.info->raster_work_counter, 1u);
+		s.bin = w < (uint32_t(p.bin_count) << tsh) ? int(p.raster_work[w >> tsh]) : -1;
+		s.tile = int(w & ((1u << tsh) - 1u));
 		s.view = 0;
 	}
 	__device__ __forceinline__ const FrameParams& view(RasterSmem&) const { return p; }
@@ -779,7 +783,7 @@ struct BatchWork {
 	__device__ __forceinline__ void next(RasterSmem& s) const {
 		const int w = int(atomicAdd(counter, 1u));
 		const int nv1 = num_views + 1;
-		int bin = -1, view = -1, base = 0;
+		int bin = -1, view = -1, tile = 0, base = 0;
 		for(int L = 0; L < 3; L++) {
 			const int* pre = level_prefix + L * nv1;
 			const int n = pre[num_views];
@@ -793,17 +797,22 @@ struct BatchWork {
 					else
 						hi = mid - 1;
 				}
+				// the prefixes count tiles (1 or 4 per bin of the view)
+				const int tsh = 2 * (views[lo].bin_shift - kBinShift);
 				const int* ph = level_prefix, *pl = level_prefix + nv1;
-				const int nhigh = ph[lo + 1] - ph[lo], nlow = pl[lo + 1] - pl[lo];
+				const int nhigh = (ph[lo + 1] - ph[lo]) >> tsh, nlow = (pl[lo + 1] - pl[lo]) >> tsh;
 				const int k = j - pre[lo];
-				const int pos = L == 0 ? k : L == 1 ? nhigh + k : nhigh + nlow + k;
+				const int kb = k >> tsh;
+				const int pos = L == 0 ? kb : L == 1 ? nhigh + kb : nhigh + nlow + kb;
 				view = lo;
+				tile = k & ((1 << tsh) - 1);
 				bin = int(views[lo].raster_work[pos]);
 				break;
 			}
 			base += n;
 		}
 		s.bin = bin;
+		s.tile = tile;
 		s.view = view;
 	}
 	// called by every thread after the barrier that follows next()
@@ -883,9 +892,16 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 		const float4 bg = make_float4(p.cfg.background_color[0], p.cfg.background_color[1],
 									  p.cfg.background_color[2], p.cfg.background_color[3]);
 		const bool dump = p.dump_counts != nullptr;
+		// the tile's origin: bins of 1 << bin_shift pixels, rastered as 32x32 tiles
 		const int bx = bin % p.bin_count_x, by = bin / p.bin_count_x;
-		const int bin_x = bx * kBinSize, bin_y = by * kBinSize;
+		const int tiled = p.bin_shift > kBinShift;
+		const int bin_x = (bx << p.bin_shift) + (s.tile & 1) * kBinSize;
+		const int bin_y = (by << p.bin_shift) + (s.tile >> 1) * kBinSize;
 		const int vis_w = p.width - bin_x, vis_h = p.height - bin_y;
+		if(vis_w <= 0 || vis_h <= 0) {
+			__syncthreads(); // every thread has read this item before thread 0 fetches the next
+			continue;
+		}
 		const int qc = int(binQuadCounts(p, bin)), tc = int(binTriCounts(p, bin));
 		const uint32_t qoff = binQuadOffsets(p, bin), toff = binTriOffsets(p, bin);
 		bool lists_ok = uint64_t(qoff) + qc <= uint64_t(p.max_bin_refs) &&
@@ -904,6 +920,15 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 				tri = (e & 0x0fffffffu) * 2 + second;
 			} else {
 				tri = p.bin_tris[toff + (i - 2 * qc)];
+			}
+			if(tiled) {
+				// a 64-pixel bin's lists hold tris of all four tiles: keep those whose quad's
+				// 32-pixel bin AABB (setup's) holds this tile
+				int x0, y0, x1, y1;
+				decodeAABB28(__ldg(p.quad_aabbs + (tri >> 1)), x0, y0, x1, y1);
+				const int tx = bin_x >> kBinShift, ty = bin_y >> kBinShift;
+				if(tx < x0 || tx > x1 || ty < y0 || ty > y1)
+					continue;
 			}
 			uint4 r0 = __ldg(p.tri_scan + size_t(tri) * 2);
 			uint4 r1 = __ldg(p.tri_scan + size_t(tri) * 2 + 1);
@@ -2231,7 +2256,8 @@ __global__ void __launch_bounds__(kMaxBatchViews) batchPlanKernel(const FramePar
 	const int v = threadIdx.x;
 	const int levels[3] = {LUCID_BIN_LEVEL_HIGH, LUCID_BIN_LEVEL_LOW, LUCID_BIN_LEVEL_EMPTY};
 	for(int L = 0; L < 3; L++) {
-		int n = v < num_views ? int(views[v].info->bin_level_counts[levels[L]]) : 0;
+		// tiles: 1 per 32-pixel bin, 4 per 64-pixel bin
+		int n = v < num_views ? int(views[v].info->bin_level_counts[levels[L]]) << (2 * (views[v].bin_shift - kBinShift)) : 0;
 		int total;
 		int off = blockExclusiveScan(n, s_scan, &total);
 		if(v < num_views)

@@ -120,14 +120,16 @@ class LucidRenderer:
     * slab_fragments: fragments per unfinished pixel that a depth slab of the raster's per-pixel
       histograms aims at (0 = 180);
     * light_max_pixel: bins whose pixels have at most this many fragments take the light raster
-      path (0 = 64, < 0 = off).
+      path (0 = 64, < 0 = off);
+    * bin_size: 32 or 64 pixels per bin side (64-pixel bins are rastered as four 32x32 tiles).
     """
 
     def __init__(self, width: int, height: int, *, max_input_quads: int | None = None,
                  max_visible_quads: int | None = None, max_bin_refs: int | None = None,
                  band_capacity: int | None = None, flags: int = 0, low_high_threshold: int = 1024,
                  raster_ctas_per_sm: int = 0, binning_ctas: int = 0, max_views: int = 1,
-                 grad_store_fragments: int = 0, slab_fragments: int = 0, light_max_pixel: int = 0):
+                 grad_store_fragments: int = 0, slab_fragments: int = 0, light_max_pixel: int = 0,
+                 bin_size: int = 32):
         if not torch.cuda.is_available():
             raise RuntimeError("lucid_gb300 needs a CUDA device")
         self.lib = _lib.load()
@@ -148,16 +150,22 @@ class LucidRenderer:
         o.grad_store_fragments = int(grad_store_fragments)
         o.slab_fragments = int(slab_fragments)
         o.light_max_pixel = int(light_max_pixel)
+        o.bin_size = int(bin_size)
         self.options = o
         self.width, self.height = int(width), int(height)
-        self.bin_count_x = (self.width + 31) // 32
-        self.bin_count_y = (self.height + 31) // 32
-        self.num_bins = self.bin_count_x * self.bin_count_y
+        self._set_bin_size(int(bin_size))
         torch.cuda.current_device()  # make sure the primary context exists
         h = ctypes.c_void_p()
         check(self.lib.lucid_create(ctypes.byref(o), self.width, self.height, ctypes.byref(h)),
               "lucid_create")
         self.handle = h
+
+    def _set_bin_size(self, bin_size: int):
+        """The bin grid of the renderer's frames (lucid_get_info's counters follow it)."""
+        self.bin_size = bin_size
+        self.bin_count_x = (self.width + bin_size - 1) // bin_size
+        self.bin_count_y = (self.height + bin_size - 1) // bin_size
+        self.num_bins = self.bin_count_x * self.bin_count_y
 
     # -- lifetime -------------------------------------------------------------------------
     def close(self):
@@ -243,7 +251,8 @@ class LucidRenderer:
         fi = frame.c_struct()
         check(self.lib.lucid_autotune(self.handle, ctypes.byref(fi), _dptr(scratch), ctypes.byref(t),
                                       _stream_ptr(stream)), "lucid_autotune")
-        return {k: getattr(t, k) for k in ("pixel_blend", "low_high_threshold", "binning_ctas",
+        self._set_bin_size(int(t.bin_size))
+        return {k: getattr(t, k) for k in ("bin_size", "pixel_blend", "low_high_threshold", "binning_ctas",
                                            "light_max_pixel", "num_candidates", "frame_ms", "default_ms")}
 
     def render_batch(self, frames, outs=None, stream=None):
