@@ -237,7 +237,7 @@ typedef struct lucid_options {
 	                               * demand, > 0 = fixed capacity, < 0 = none (the backward pass
 	                               * recomputes the fragment lists instead of reading them)      */
 	int32_t slab_fragments;    /* raster: fragments per unfinished pixel a depth slab aims at
-	                            * (0 = 180; a large value counts every key at once)            */
+	                            * (0 = 165; a large value counts every key at once)            */
 	int32_t light_max_pixel;   /* raster: a bin whose pixels have at most this many fragments
 	                            * takes the light path (one warp per row, passes of the 32
 	                            * nearest fragments per pixel, stop at T == 0); deeper bins take

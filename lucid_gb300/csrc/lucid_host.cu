@@ -186,7 +186,7 @@ void setShadingInputs(FrameParams& p, const lucid_frame_inputs* in) {
 }
 
 // fragments per unfinished pixel that a depth slab of the raster aims at
-int slabTarget(const lucid_renderer* r) { return r->opts.slab_fragments > 0 ? r->opts.slab_fragments : 180; }
+int slabTarget(const lucid_renderer* r) { return r->opts.slab_fragments > 0 ? r->opts.slab_fragments : 165; }
 // deepest pixel of a bin that takes the light raster path (-1: none)
 int lightMaxPixel(const lucid_options* o) {
 	return o->light_max_pixel == 0 ? 64 : (o->light_max_pixel < 0 ? -1 : o->light_max_pixel);

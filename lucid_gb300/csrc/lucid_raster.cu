@@ -381,7 +381,7 @@ __device__ void writePixel(const FrameParams& p, int px, int py, float4 c) {
 // only entries whose range meets the current window of some pixel of the row are visited; the
 // window of pixel t holds the keys of its buckets [px_lo, px_cut] (bucket = (key - kmin) >> shift).
 // With `ekeys` and flo <= fhi, entries are culled against the fixed key range [flo, fhi] instead.
-template <bool kQuad = false, typename Fn>
+template <bool kQuad = false, int U = 4, typename Fn>
 __device__ __forceinline__ void forEachGroupFragment(const FrameParams& p, const RasterSmem& s,
 													  const uint2* scratch, const float4* planes, int band_cap, int bin_x,
 													  int bin_y, int p0, int p1, Fn fn,
@@ -469,38 +469,38 @@ __device__ __forceinline__ void forEachGroupFragment(const FrameParams& p, const
 		if(LUCID_RASTER_COUNTERS && ecount && lane == 0)
 			*ecount += __popc(todo);
 		while(todo != 0u) {
-			int k[4];
-			bool has[4];
+			int k[U];
+			bool has[U];
 #pragma unroll
-			for(int u = 0; u < 4; u++) {
+			for(int u = 0; u < U; u++) {
 				has[u] = todo != 0u;
 				k[u] = has[u] ? __ffs(todo) - 1 : 0;
 				if(has[u])
 					todo &= todo - 1u;
 			}
-			uint32_t sp[4], tr[4], key[4];
-			float kdx[4], kty[4];
+			uint32_t sp[U], tr[U], key[U];
+			float kdx[U], kty[U];
 #pragma unroll
-			for(int u = 0; u < 4; u++) {
+			for(int u = 0; u < U; u++) {
 				sp[u] = __shfl_sync(0xffffffffu, span, k[u]);
 				kdx[u] = __shfl_sync(0xffffffffu, dx, k[u]);
 				kty[u] = __shfl_sync(0xffffffffu, ty, k[u]);
 				tr[u] = __shfl_sync(0xffffffffu, tri, k[u]);
 			}
 #pragma unroll
-			for(int u = 0; u < 4; u++)
+			for(int u = 0; u < U; u++)
 				key[u] = nearFirstKey(kdx[u] * fx + kty[u]);
 			if constexpr(kQuad) {
-				// the four entries' fragments of this lane in one call (the callback can issue
+				// the U entries' fragments of this lane in one call (the callback can issue
 				// their shared-memory atomics back to back)
-				bool on[4];
+				bool on[U];
 #pragma unroll
-				for(int u = 0; u < 4; u++)
+				for(int u = 0; u < U; u++)
 					on[u] = has[u] && in_group && lane >= int(sp[u] & 31u) && lane <= int(sp[u] >> 5);
 				fn(t, on, key, tr);
 			} else {
 #pragma unroll
-				for(int u = 0; u < 4; u++)
+				for(int u = 0; u < U; u++)
 					if(has[u] && in_group && lane >= int(sp[u] & 31u) && lane <= int(sp[u] >> 5))
 						fn(t, key[u], tr[u]);
 			}
@@ -1366,15 +1366,16 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 #if LUCID_RASTER_COUNTERS
 				const long long tw0 = clock64();
 #endif
-				forEachGroupFragment<true>(p, s, scratch, planes, band_cap, bin_x, bin_y, p0, p1,
+				constexpr int AU = 4; // entries per step (8 measured slower)
+				forEachGroupFragment<true, AU>(p, s, scratch, planes, band_cap, bin_x, bin_y, p0, p1,
 										   [&](int tp, const bool* on, const uint32_t* key, const uint32_t* tri) {
 											   const int end = (tp + 1) * rcap;
-											   int pos[4];
+											   int pos[AU];
 #pragma unroll
-											   for(int u = 0; u < 4; u++)
+											   for(int u = 0; u < AU; u++)
 												   pos[u] = on[u] && key[u] >= lo_k && key[u] <= hi_k ? atomicAdd(&s.px_wend[tp], 1) : end;
 #pragma unroll
-											   for(int u = 0; u < 4; u++)
+											   for(int u = 0; u < AU; u++)
 												   if(pos[u] < end) {
 													   s.kv[1][0][pos[u]] = key[u];
 													   s.kv[1][1][pos[u]] = fragPayload(tp, tri[u]);

@@ -118,7 +118,7 @@ class LucidRenderer:
     * grad_store_fragments: fragment store of the differentiable frame (0 grows on demand, < 0
       none);
     * slab_fragments: fragments per unfinished pixel that a depth slab of the raster's per-pixel
-      histograms aims at (0 = 180);
+      histograms aims at (0 = 165);
     * light_max_pixel: bins whose pixels have at most this many fragments take the light raster
       path (0 = 64, < 0 = off);
     * bin_size: 32 or 64 pixels per bin side (64-pixel bins are rastered as four 32x32 tiles).
