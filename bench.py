@@ -367,6 +367,9 @@ def batch_bench(steps, warmup, flush_buf, num_views=64):
                                        max_bin_refs=8 * nq)
     br = LucidRenderer(max(v.width for v in views), max(v.height for v in views), max_input_quads=total_quads,
                        max_visible_quads=total_quads, max_bin_refs=4 * total_quads, max_views=num_views)
+    # the batch's options (bin size, per-bin raster path, LOW/HIGH threshold, binning CTAs) tuned
+    # on the batch itself by lucid_autotune_batch (the plain arm keeps the defaults)
+    tuned = br.autotune_batch(frames, outs=outs)
     stream = torch.cuda.current_stream()
 
     def run_plain():
@@ -402,7 +405,7 @@ def batch_bench(steps, warmup, flush_buf, num_views=64):
             "views": num_views, "triangles": int(sum(v.num_tris for v in views)), "fragments": frags,
             "plain_ms": t_plain, "batch_ms": t_batch, "plain_frames_per_s": num_views / (t_plain / 1e3),
             "batch_frames_per_s": num_views / (t_batch / 1e3), "speedup": t_plain / t_batch,
-            "view_errors": errors, "median_of": steps}
+            "view_errors": errors, "median_of": steps, "tuning": tuned}
 
 
 def quadgen_bench(steps, warmup):

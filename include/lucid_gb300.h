@@ -455,7 +455,8 @@ typedef struct lucid_tuning {
 /* Autotuner (no reference counterpart): times lucid_render of `inputs` into scratch_rgba
  * (device, width*height*4 floats) under candidate configurations, by coordinate descent over
  * the bin size (32 or 64 pixels; not in the reference-order mode), the blend strategy
- * (raster-pass blend or LUCID_OPT_PIXEL_BLEND), the LOW/HIGH threshold (256, 1024, 4096), the
+ * (raster-pass blend or LUCID_OPT_PIXEL_BLEND; not for renderers with options.max_views > 1,
+ * whose batches blend in the raster pass), the LOW/HIGH threshold (256, 1024, 4096), the
  * binning CTAs (1 or 2 per SM, within options.binning_ctas) and the per-bin raster path
  * (options.light_max_pixel: -1, 32, 64, 128, 256; bins up to that depth are rastered one warp
  * per row, deeper ones by CTA-wide depth windows); CUDA events on `stream`, median of 3 frames
@@ -463,6 +464,14 @@ typedef struct lucid_tuning {
  * *out (may be NULL). Synchronous. Raster CTAs are one per SM (shared memory). */
 lucid_status lucid_autotune(lucid_renderer* renderer, const lucid_frame_inputs* inputs,
 							float* scratch_rgba, lucid_tuning* out, void* stream);
+
+/* Autotuner of batched frames (no reference counterpart): the same coordinate descent as
+ * lucid_autotune (bin size, LOW/HIGH threshold, binning CTAs, per-bin raster path; not the
+ * blend strategy), timing lucid_render_batch of `views` (which it renders into their
+ * out_rgba). A batch's best options are not those of any one of its views: deep small views
+ * and shallow large ones pull the per-bin raster path different ways. Synchronous. */
+lucid_status lucid_autotune_batch(lucid_renderer* renderer, const lucid_view* views, int32_t num_views,
+								  lucid_tuning* out, void* stream);
 
 /* Quad generator (replaces triNeighbours / quadNodes / genQuads, src/quad_generator.cpp:18-201,
  * as used by Scene::generateQuads, src/scene.cpp:237-246): pairs triangles that share an edge

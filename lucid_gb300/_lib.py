@@ -132,6 +132,8 @@ SIGNATURES = [
     ("lucid_get_batch_info", c_int32, [c_void_p, c_int32, ctypes.POINTER(Info), c_void_p]),
     ("lucid_autotune", c_int32, [c_void_p, ctypes.POINTER(FrameInputsC), c_void_p,
                                  ctypes.POINTER(Tuning), c_void_p]),
+    ("lucid_autotune_batch", c_int32, [c_void_p, ctypes.POINTER(ViewC), c_int32,
+                                       ctypes.POINTER(Tuning), c_void_p]),
     ("lucid_quad_generate", c_int32, [c_void_p, c_int32, c_void_p, c_int32, ctypes.c_float, c_void_p,
                                       ctypes.POINTER(c_int32), ctypes.POINTER(c_int32), c_void_p]),
     ("lucid_bin_noalloc", c_int32, [c_void_p, c_void_p, c_int32, c_int32, c_int32, c_int32,

@@ -7,6 +7,7 @@
 // device), so a frame needs no indirect dispatch and can be captured in a CUDA graph.
 
 #include <algorithm>
+#include <functional>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -1076,9 +1077,12 @@ int viewBinningCtas(const lucid_renderer* r, int nq) {
 
 std::vector<int64_t> batchKey(const lucid_renderer* r, const lucid_view* views, int n) {
 	std::vector<int64_t> key;
-	key.reserve(2 + 4 * size_t(n));
+	key.reserve(4 + 4 * size_t(n));
 	key.push_back(n);
+	// options the recorded graph bakes in (grid shapes, the sort pass)
 	key.push_back(r->opts.bin_size);
+	key.push_back(r->opts.binning_ctas);
+	key.push_back(int64_t(r->opts.flags & LUCID_OPT_SORTED_BIN_LISTS));
 	for(int v = 0; v < n; v++) {
 		key.push_back(views[v].width);
 		key.push_back(views[v].height);
@@ -1334,14 +1338,13 @@ extern "C" lucid_status lucid_get_batch_info(lucid_renderer* r, int32_t view, lu
 	return LUCID_OK;
 }
 
-extern "C" lucid_status lucid_autotune(lucid_renderer* r, const lucid_frame_inputs* in,
-									   float* scratch_rgba, lucid_tuning* out, void* stream) {
-	if(!r || !scratch_rgba)
-		return fail(LUCID_INVALID_ARG, "lucid_autotune: renderer and scratch_rgba are required");
-	lucid_status st = validateInputs(r, in);
-	if(st != LUCID_OK)
-		return st;
-	cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+namespace {
+
+// Coordinate descent over the renderer's options, timing `frame` (one lucid_render or one
+// lucid_render_batch): CUDA events on `s`, median of 3 after a warm-up call per candidate. The
+// winner stays in r->opts; on failure the options are restored.
+lucid_status autotuneCore(lucid_renderer* r, cudaStream_t s, bool pixel_blend_candidate,
+						  const std::function<lucid_status()>& frame, lucid_tuning* out) {
 	cudaEvent_t e0, e1;
 	LUCID_CUDA_TRY(cudaEventCreate(&e0));
 	cudaError_t cerr = cudaEventCreate(&e1);
@@ -1351,12 +1354,11 @@ extern "C" lucid_status lucid_autotune(lucid_renderer* r, const lucid_frame_inpu
 	}
 	const lucid_options saved = r->opts;
 	int candidates = 0;
-	// median of 3 timed frames after one warm-up frame; < 0 on failure
 	auto timeFrame = [&](float& ms) -> lucid_status {
 		float t[3];
 		for(int i = 0; i < 4; i++) {
 			cudaEventRecord(e0, s);
-			lucid_status rs = lucid_render(r, in, scratch_rgba, stream);
+			lucid_status rs = frame();
 			if(rs != LUCID_OK)
 				return rs;
 			cudaEventRecord(e1, s);
@@ -1372,6 +1374,7 @@ extern "C" lucid_status lucid_autotune(lucid_renderer* r, const lucid_frame_inpu
 		return LUCID_OK;
 	};
 	float best_ms = 0.0f, default_ms = 0.0f;
+	lucid_status st;
 	if((st = timeFrame(default_ms)) == LUCID_OK) {
 		best_ms = default_ms;
 		lucid_options best = r->opts;
@@ -1391,10 +1394,10 @@ extern "C" lucid_status lucid_autotune(lucid_renderer* r, const lucid_frame_inpu
 			o.bin_size = best.bin_size == 64 ? 32 : 64;
 			st = tryOpts(o);
 		}
-		// 1. blend strategy
+		// 1. blend strategy (not for batches: lucid_render_batch blends in the raster pass)
 		o = best;
 		o.flags ^= LUCID_OPT_PIXEL_BLEND;
-		if(st == LUCID_OK)
+		if(st == LUCID_OK && pixel_blend_candidate)
 			st = tryOpts(o);
 		// 2. LOW/HIGH threshold (raster work order)
 		for(int th : {256, 1024, 4096}) {
@@ -1441,4 +1444,27 @@ extern "C" lucid_status lucid_autotune(lucid_renderer* r, const lucid_frame_inpu
 		out->default_ms = default_ms;
 	}
 	return LUCID_OK;
+}
+
+} // namespace
+
+extern "C" lucid_status lucid_autotune(lucid_renderer* r, const lucid_frame_inputs* in,
+									   float* scratch_rgba, lucid_tuning* out, void* stream) {
+	if(!r || !scratch_rgba)
+		return fail(LUCID_INVALID_ARG, "lucid_autotune: renderer and scratch_rgba are required");
+	lucid_status st = validateInputs(r, in);
+	if(st != LUCID_OK)
+		return st;
+	return autotuneCore(r, reinterpret_cast<cudaStream_t>(stream), r->opts.max_views <= 1,
+						[&]() { return lucid_render(r, in, scratch_rgba, stream); }, out);
+}
+
+extern "C" lucid_status lucid_autotune_batch(lucid_renderer* r, const lucid_view* views, int32_t num_views,
+											 lucid_tuning* out, void* stream) {
+	if(!r || !views || num_views <= 0)
+		return fail(LUCID_INVALID_ARG, "lucid_autotune_batch: renderer, views and num_views > 0 are required");
+	if(r->opts.flags & (LUCID_OPT_REFERENCE_ORDER | LUCID_OPT_PIXEL_BLEND))
+		return fail(LUCID_NOT_SUPPORTED, "lucid_autotune_batch: batches render the exact order with the raster-pass blend");
+	return autotuneCore(r, reinterpret_cast<cudaStream_t>(stream), false,
+						[&]() { return lucid_render_batch(r, views, num_views, stream); }, out);
 }

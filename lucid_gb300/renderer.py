@@ -255,9 +255,7 @@ class LucidRenderer:
         return {k: getattr(t, k) for k in ("bin_size", "pixel_blend", "low_high_threshold", "binning_ctas",
                                            "light_max_pixel", "num_candidates", "frame_ms", "default_ms")}
 
-    def render_batch(self, frames, outs=None, stream=None):
-        """Renders every (frame, width, height) of `frames` with lucid_render_batch; returns the
-        output images (allocated unless `outs` is given)."""
+    def _views(self, frames, outs):
         n = len(frames)
         if outs is None:
             outs = [torch.empty((h, w, 4), dtype=torch.float32, device="cuda") for _, w, h in frames]
@@ -267,8 +265,26 @@ class LucidRenderer:
             views[i].inputs = frame.c_struct()
             views[i].out_rgba = out.data_ptr()
         self._batch_keep = (frames, outs)
-        check(self.lib.lucid_render_batch(self.handle, views, n, _stream_ptr(stream)), "lucid_render_batch")
+        return views, outs
+
+    def render_batch(self, frames, outs=None, stream=None):
+        """Renders every (frame, width, height) of `frames` with lucid_render_batch; returns the
+        output images (allocated unless `outs` is given)."""
+        views, outs = self._views(frames, outs)
+        check(self.lib.lucid_render_batch(self.handle, views, len(frames), _stream_ptr(stream)),
+              "lucid_render_batch")
         return outs
+
+    def autotune_batch(self, frames, outs=None, stream=None) -> dict:
+        """Runs lucid_autotune_batch on the views of `frames` (rendered into `outs`); the winner
+        stays in the renderer."""
+        views, outs = self._views(frames, outs)
+        t = _lib.Tuning()
+        check(self.lib.lucid_autotune_batch(self.handle, views, len(frames), ctypes.byref(t),
+                                            _stream_ptr(stream)), "lucid_autotune_batch")
+        self._set_bin_size(int(t.bin_size))
+        return {k: getattr(t, k) for k in ("bin_size", "pixel_blend", "low_high_threshold", "binning_ctas",
+                                           "light_max_pixel", "num_candidates", "frame_ms", "default_ms")}
 
     def batch_info(self, view: int, stream=None):
         info = _lib.Info()

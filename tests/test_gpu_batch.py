@@ -135,3 +135,46 @@ def test_batch_views_match_oracle(gpu, oracle):
         assert int(info.num_fragments) == o["num_fragments"], i
         assert tuple(info.num_visible_quads) == tuple(o["num_visible"]), i
     r.close()
+
+
+def test_batch_after_single_view_autotune(gpu):
+    """A batch renderer tuned on one of its views (the bench's C3 arm) still renders every view
+    exactly: the tuner leaves the pixel-parallel blend out for batch renderers."""
+    from lucid_gb300.renderer import FrameInputs
+    views = _mixed_views()[:4]
+    r = _batch_renderer(views)
+    frames = [(FrameInputs.from_scene(v), v.width, v.height) for v in views]
+    full = [i for i, v in enumerate(views) if (v.width, v.height) == (r.width, r.height)]
+    assert full
+    tuned = r.autotune(frames[full[0]][0])
+    assert tuned["pixel_blend"] == 0
+    imgs = r.render_batch(frames)
+    # the tuned bin size and LOW/HIGH threshold change the bin statistics, not the frame
+    for i, sc in enumerate(views):
+        ref, rinfo = _single(sc)
+        np.testing.assert_array_equal(imgs[i].cpu().numpy(), ref, err_msg=f"view {i}")
+        binfo = r.batch_info(i)
+        assert binfo.error_code == 0, (i, binfo.error_code)
+        assert int(binfo.num_fragments) == int(rinfo.num_fragments), i
+        assert int(binfo.max_pixel_fragments) == int(rinfo.max_pixel_fragments), i
+    r.close()
+
+
+def test_autotune_batch(gpu):
+    """lucid_autotune_batch times the batch itself; the tuned batch renders every view exactly."""
+    from lucid_gb300.renderer import FrameInputs
+    views = _mixed_views()
+    r = _batch_renderer(views)
+    frames = [(FrameInputs.from_scene(v), v.width, v.height) for v in views]
+    tuned = r.autotune_batch(frames)
+    assert tuned["pixel_blend"] == 0 and tuned["bin_size"] in (32, 64)
+    assert tuned["num_candidates"] >= 8
+    assert tuned["frame_ms"] <= tuned["default_ms"]
+    imgs = r.render_batch(frames)
+    for i, sc in enumerate(views):
+        ref, rinfo = _single(sc)
+        np.testing.assert_array_equal(imgs[i].cpu().numpy(), ref, err_msg=f"view {i}")
+        binfo = r.batch_info(i)
+        assert binfo.error_code == 0, (i, binfo.error_code)
+        assert int(binfo.num_fragments) == int(rinfo.num_fragments), i
+    r.close()
