@@ -296,3 +296,69 @@ def quadgen(positions, tris, square_weight=1.0, order=0):
     if rc != 0:
         raise RuntimeError(f"oracle_quadgen failed ({rc})")
     return out[:n.value], nd.value
+
+
+def _bind_ref(L):
+    if not hasattr(L, "_ref_bound"):
+        L.oracle_ref_shade.argtypes = [ctypes.POINTER(OracleInputs), ctypes.c_int32] + [ctypes.c_void_p] * 5
+        L.oracle_ref_shade.restype = ctypes.c_int
+        L.oracle_ref_reduce.argtypes = [ctypes.c_void_p, ctypes.c_int32] + [ctypes.c_void_p] * 4
+        L.oracle_ref_reduce.restype = ctypes.c_int
+        L.oracle_ref_pow.argtypes = [ctypes.c_float, ctypes.c_float]
+        L.oracle_ref_pow.restype = ctypes.c_float
+        L._ref_bound = True
+
+
+def ref_pow_address():
+    """Address of the oracle's pow (oracle_ref_pow), for the reference harness's GLSL pow."""
+    L = lib()
+    _bind_ref(L)
+    return ctypes.cast(L.oracle_ref_pow, ctypes.c_void_p).value
+
+
+def ref_shade(scene, px, py, tris, max_visible_quads=None):
+    """The reference-order mode's shading (shadeRef) of samples (px[i], py[i], tris[i]) after the
+    oracle's setup of `scene`: RGBA8 colours (uint32) and depths (float32)."""
+    L = lib()
+    _bind_ref(L)
+    mvq = max_visible_quads or max(1024, scene.num_quads)
+    keep = []
+    positions = np.ascontiguousarray(scene.positions, dtype=np.float32)
+    colors = np.ascontiguousarray(scene.colors)
+    quads = np.ascontiguousarray(scene.quads, dtype=np.uint32)
+    inst = np.ascontiguousarray(scene.instances, dtype=np.int32)
+    icol = np.ascontiguousarray(scene.instance_colors, dtype=np.uint32)
+    opac = None if scene.tri_opacity is None else np.ascontiguousarray(scene.tri_opacity, np.float32)
+    keep += [positions, colors, quads, inst, icol, opac]
+    ins = OracleInputs(
+        **_shading_inputs(scene, keep), width=scene.width, height=scene.height, max_visible_quads=mvq,
+        low_high_threshold=1024, flags=0, order_mode=1, positions=_ptr(positions), colors=_ptr(colors),
+        color_format=scene.color_format, num_verts=positions.shape[0], quads_ib=_ptr(quads),
+        num_quads=quads.shape[0], num_instances=inst.shape[0], instances=_ptr(inst),
+        instance_colors=_ptr(icol), tri_opacity=_ptr(opac), config=ctypes.addressof(scene.config),
+        bin_subset=None, num_bin_subset=0, num_threads=1)
+    px = np.ascontiguousarray(px, np.int32)
+    py = np.ascontiguousarray(py, np.int32)
+    tris = np.ascontiguousarray(tris, np.uint32)
+    out_c = np.zeros(len(tris), np.uint32)
+    out_d = np.zeros(len(tris), np.float32)
+    if L.oracle_ref_shade(ctypes.byref(ins), len(tris), px.ctypes.data, py.ctypes.data, tris.ctypes.data,
+                          out_c.ctypes.data, out_d.ctypes.data) != 0:
+        raise RuntimeError("oracle_ref_shade failed")
+    return out_c, out_d
+
+
+def ref_reduce(background, colors, depths, seg):
+    """One pixel's samples through the reference-order mode's 3-deep window (RefReduce):
+    RGBA float32[4]."""
+    L = lib()
+    _bind_ref(L)
+    bg = np.ascontiguousarray(background, np.float32)
+    c = np.ascontiguousarray(colors, np.uint32)
+    d = np.ascontiguousarray(depths, np.float32)
+    s = np.ascontiguousarray(seg, np.int32)
+    out = np.zeros(4, np.float32)
+    if L.oracle_ref_reduce(bg.ctypes.data, len(c), c.ctypes.data, d.ctypes.data, s.ctypes.data,
+                           out.ctypes.data) != 0:
+        raise RuntimeError("oracle_ref_reduce failed")
+    return out

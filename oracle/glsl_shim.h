@@ -1,7 +1,9 @@
 /*
  * GLSL-in-C++ shim: just enough of the GLSL language (vector/matrix types, swizzles, built-in
- * functions, integer/float conversions) to compile the reference's own setup functions
- * (data/shaders/quad_setup.glsl, shared/funcs.glsl) as plain C++ on the CPU.
+ * functions, integer/float conversions, single-invocation subgroup operations) to compile the
+ * reference's own setup, binning, row-span, shading and reduction functions
+ * (data/shaders/quad_setup.glsl, bin_counter.glsl, raster_low.glsl, shared/*.glsl) as plain C++
+ * on the CPU.
  *
  * TEST INFRASTRUCTURE ONLY: used by oracle/ref_build.py to build oracle/_ref, which pins the
  * oracle's setup records to the reference's source. Nothing in lucid_gb300/ uses it.
@@ -36,6 +38,7 @@ template <class T, int N, int M> struct Swz {
 			base[idx[k]] = base[idx[k]] * T(s);
 		return *this;
 	}
+	Swz& operator=(const vecN<T, M>& v);
 };
 
 template <class T, int N> struct vecN;
@@ -75,6 +78,8 @@ template <class T> struct vecN<T, 4> {
 	vecN<T, 2> zw() const { return vecN<T, 2>(z, w); }
 	Swz<T, 4, 3> xyz() { return Swz<T, 4, 3>{&x, {0, 1, 2}}; }
 	vecN<T, 3> xyz() const { return vecN<T, 3>(x, y, z); }
+	Swz<T, 4, 3> rgb() { return Swz<T, 4, 3>{&x, {0, 1, 2}}; }
+	vecN<T, 3> rgb() const { return vecN<T, 3>(x, y, z); }
 	vecN<T, 3> xzw() const { return vecN<T, 3>(x, z, w); }
 };
 
@@ -83,6 +88,11 @@ template <class T, int N, int M> Swz<T, N, M>::operator vecN<T, M>() const {
 	for(int k = 0; k < M; k++)
 		r[k] = base[idx[k]];
 	return r;
+}
+template <class T, int N, int M> Swz<T, N, M>& Swz<T, N, M>::operator=(const vecN<T, M>& v) {
+	for(int k = 0; k < M; k++)
+		base[idx[k]] = v[k];
+	return *this;
 }
 
 typedef vecN<float, 2> vec2;
@@ -118,6 +128,25 @@ LUCID_SHIM_BINOP(-)
 LUCID_SHIM_BINOP(*)
 LUCID_SHIM_BINOP(/)
 #undef LUCID_SHIM_BINOP
+
+// scalar on the left: componentwise s OP v[i]
+#define LUCID_SHIM_SCALAR_LEFT(OP)                                                                    \
+	template <class T, int N> vecN<T, N> operator OP(T s, const vecN<T, N>& a) {                       \
+		vecN<T, N> r;                                                                                  \
+		for(int i = 0; i < N; i++)                                                                     \
+			r[i] = s OP a[i];                                                                          \
+		return r;                                                                                      \
+	}
+LUCID_SHIM_SCALAR_LEFT(+)
+LUCID_SHIM_SCALAR_LEFT(-)
+LUCID_SHIM_SCALAR_LEFT(*)
+#undef LUCID_SHIM_SCALAR_LEFT
+
+// a swizzle in an expression reads as its vector
+template <class T, int N, int M> vecN<T, M> swzValue(const Swz<T, N, M>& s) { return vecN<T, M>(s); }
+template <class T, int N, int M> vecN<T, M> operator-(const Swz<T, N, M>& s) { return -swzValue(s); }
+template <class T, int N, int M, class U> auto operator*(const Swz<T, N, M>& a, const U& b) { return swzValue(a) * b; }
+template <class T, int N, int M> vecN<T, M> operator*(T b, const Swz<T, N, M>& a) { return b * swzValue(a); }
 
 template <class T, int N> vecN<T, N> operator-(const vecN<T, N>& a) {
 	vecN<T, N> r;
@@ -176,6 +205,16 @@ template <int N> vecN<float, N> max(const vecN<float, N>& a, const vecN<float, N
 template <int N> vecN<float, N> clamp(const vecN<float, N>& v, const vecN<float, N>& lo, const vecN<float, N>& hi) {
 	return min(max(v, lo), hi);
 }
+// clamp(v, 0.0, 1.0) of a float vector (SATURATE): min(max(v, lo), hi) per component
+template <int N> vecN<float, N> clamp(const vecN<float, N>& v, double lo, double hi) {
+	return min(max(v, vecN<float, N>(float(lo))), vecN<float, N>(float(hi)));
+}
+template <int N> vecN<float, N> fract(const vecN<float, N>& v) {
+	vecN<float, N> r;
+	for(int i = 0; i < N; i++)
+		r[i] = v[i] - std::floor(v[i]);
+	return r;
+}
 inline float min(float a, int b) { return std::fmin(a, float(b)); }
 inline float max(float a, int b) { return std::fmax(a, float(b)); }
 inline int clamp(int v, int lo, int hi) { return min(max(v, lo), hi); }
@@ -200,6 +239,33 @@ inline float uintBitsToFloat(uint u) {
 }
 inline vec3 uintBitsToFloat(const uvec3& v) {
 	return vec3(uintBitsToFloat(v.x), uintBitsToFloat(v.y), uintBitsToFloat(v.z));
+}
+inline vec2 uintBitsToFloat(const uvec2& v) { return vec2(uintBitsToFloat(v.x), uintBitsToFloat(v.y)); }
+
+// GLSL pow is implementation-defined; the harness points this at the pow that the oracle and
+// the CUDA path share (the oracle's refPow)
+extern float (*g_pow)(float, float);
+inline float pow(float x, float y) { return g_pow(x, y); }
+
+// integer bit functions
+inline int bitCount(uint v) { return __builtin_popcount(v); }
+inline int findLSB(uint v) { return v ? __builtin_ctz(v) : -1; }
+
+// subgroup operations of one invocation running alone: a vote is its own predicate, a shuffle
+// returns its own value
+inline bool subgroupAny(bool b) { return b; }
+inline bool subgroupAll(bool b) { return b; }
+template <class T> T subgroupShuffle(const T& v, int) { return v; }
+
+// textures are outside the pinned functions: the stub marks a call, and the tests use scenes
+// without textures
+struct sampler2D {
+	int unused;
+};
+extern int g_texture_calls;
+inline vec4 textureGrad(const sampler2D&, const vec2&, const vec2&, const vec2&) {
+	g_texture_calls++;
+	return vec4(NAN);
 }
 
 // int() / uint() conversions. Of a float: truncation toward zero, saturating at the type's

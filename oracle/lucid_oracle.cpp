@@ -1563,6 +1563,49 @@ double pixelLoss64(const GradCtx& g, uint32_t pix, const double* vc, const doubl
 	return l;
 }
 
+extern "C" int oracle_ref_shade(const oracle_inputs* in, int32_t n, const int32_t* px, const int32_t* py,
+								const uint32_t* tris, uint32_t* colors, float* depths) {
+	if(!in || !in->config || in->width <= 0 || in->height <= 0 || in->max_visible_quads <= 0 || n < 0 ||
+	   (n > 0 && (!px || !py || !tris || !colors || !depths)))
+		return 1;
+	if(in->num_quads > 0 && (!in->positions || !in->quads_ib || !in->instances))
+		return 1;
+	State s;
+	initState(s, in);
+	oracle_outputs dummy;
+	memset(&dummy, 0, sizeof(dummy));
+	quadSetup(s, &dummy);
+	for(int i = 0; i < n; i++) {
+		const uint32_t tri = tris[i];
+		if(tri >= 2u * uint32_t(in->max_visible_quads))
+			return 1;
+		const uint32_t prim = s.quad_source[tri >> 1] * 2 + (tri & 1);
+		float depth = 0.0f;
+		colors[i] = shadeRef(s, tri, prim, px[i], py[i], depth);
+		depths[i] = depth;
+	}
+	return 0;
+}
+
+extern "C" int oracle_ref_reduce(const float* background, int32_t n, const uint32_t* colors, const float* depths,
+								 const int32_t* seg, float* rgba) {
+	if(!background || !rgba || n < 0 || (n > 0 && (!colors || !depths || !seg)))
+		return 1;
+	RefReduce r;
+	r.init(3, false);
+	for(int i = 0; i < n; i++) {
+		if(i > 0 && seg[i] != seg[i - 1])
+			r.endSegment();
+		r.sample(colors[i], depths[i]);
+	}
+	if(n > 0)
+		r.endSegment();
+	r.finish(background, rgba);
+	return 0;
+}
+
+extern "C" float oracle_ref_pow(float x, float y) { return refPow(x, y); }
+
 } // namespace
 
 extern "C" int oracle_version(void) { return 1; }

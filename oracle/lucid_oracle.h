@@ -103,6 +103,19 @@ int oracle_run(const oracle_inputs* in, oracle_outputs* out);
 
 int oracle_version(void);
 
+/* ---- reference-order shading and reduction, one sample or one pixel at a time ----
+ * Test entry points that pin the reference-order mode to the reference's own shadeSample,
+ * reduceSample and finishReduceSamples (tests/test_oracle_ref_pin.py).
+ * oracle_ref_shade: setup of `in`, then shadeRef of each (px[i], py[i], tris[i]): RGBA8 colour
+ * and depth (inv_ray_pos). oracle_ref_reduce: one pixel's samples through RefReduce (3-deep
+ * window) in segments seg[i] (non-decreasing; the colour is saturated at each segment's end),
+ * then finish over background[0..3]. oracle_ref_pow: the pow of the sRGB conversions. */
+int oracle_ref_shade(const oracle_inputs* in, int32_t n, const int32_t* px, const int32_t* py, const uint32_t* tris,
+					 uint32_t* colors, float* depths);
+int oracle_ref_reduce(const float* background, int32_t n, const uint32_t* colors, const float* depths,
+					  const int32_t* seg, float* rgba);
+float oracle_ref_pow(float x, float y);
+
 /* ---- FP64 gradient model (checker of lucid_render_backward) ----
  * Builds the exact per-pixel fragment lists of the scene (coverage, order and barycentric
  * weights depend on positions only, which stay frozen) and evaluates, in FP64, the loss

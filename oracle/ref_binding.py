@@ -105,3 +105,48 @@ def coverage(quad_aabbs, tri_scan, num_visible, mvq, width, height):
     L.ref_coverage(qa.ctypes.data, ts.ctypes.data, num_visible[0], num_visible[1], mvq, width, height,
                    counts.ctypes.data)
     return counts
+
+
+def _bind_shading(L):
+    if not hasattr(L, "_shading"):
+        L.ref_shade_samples.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32] + \
+            [ctypes.c_void_p] * 5
+        L.ref_shade_samples.restype = ctypes.c_int
+        L.ref_reduce.argtypes = [ctypes.c_void_p, ctypes.c_int32] + [ctypes.c_void_p] * 4
+        L.ref_reduce.restype = ctypes.c_int
+        L._shading = True
+
+
+def shade_samples(scene, px, py, tris, pow_address, max_visible_quads=None):
+    """The reference's shadeSample of samples (px[i], py[i], tris[i]) on the records of its own
+    setup of `scene` (run here first): RGBA8 colours and depths. pow_address: the pow that GLSL
+    leaves to the implementation (the oracle's). Raises if a sample reached the texture stub."""
+    L = lib()
+    _bind_shading(L)
+    quad_setup(scene, max_visible_quads)
+    icol = np.ascontiguousarray(scene.instance_colors, np.uint32)
+    px = np.ascontiguousarray(px, np.int32)
+    py = np.ascontiguousarray(py, np.int32)
+    tris = np.ascontiguousarray(tris, np.uint32)
+    colors = np.zeros(len(tris), np.uint32)
+    depths = np.zeros(len(tris), np.float32)
+    tex = L.ref_shade_samples(ctypes.addressof(scene.config), icol.ctypes.data if len(icol) else None,
+                              ctypes.c_void_p(pow_address), len(tris), px.ctypes.data, py.ctypes.data,
+                              tris.ctypes.data, colors.ctypes.data, depths.ctypes.data)
+    if tex != 0:
+        raise RuntimeError(f"{tex} samples reached the texture stub")
+    return colors, depths
+
+
+def reduce(background, colors, depths, seg):
+    """The reference's initReduceSamples / reduceSample / finishReduceSamples over one pixel's
+    samples in segments `seg`: RGBA float32[4]."""
+    L = lib()
+    _bind_shading(L)
+    bg = np.ascontiguousarray(background, np.float32)
+    c = np.ascontiguousarray(colors, np.uint32)
+    d = np.ascontiguousarray(depths, np.float32)
+    s = np.ascontiguousarray(seg, np.int32)
+    out = np.zeros(4, np.float32)
+    L.ref_reduce(bg.ctypes.data, len(c), c.ctypes.data, d.ctypes.data, s.ctypes.data, out.ctypes.data)
+    return out

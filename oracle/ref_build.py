@@ -16,6 +16,13 @@ them where they lie in the reference tree (nothing is copied into the repository
   countLargeTriBins, with the ScanlineParams loaders of shared/scanline.glsl and decodeAABB28;
 * from data/shaders/raster_low.glsl: scratchBlockRowOffset, generateRowTris, with rasterBinStep
   and the block / half-block macros of shared/raster.glsl;
+* from data/shaders/shared/shading.glsl: getTriangleParams, getTriangleVertexColors,
+  getTriangleVertexNormals, getTriangleVertexTexCoords, shadeSample, the ReductionContext struct
+  with its RC_* macros, swap, initReduceSamples, reduceSample, finishReduceSamples; with
+  decodeRGBA8, encodeRGBA8, SRGBToLinear, linearToSRGB, finalShading, the swap helpers and
+  SATURATE of shared/funcs.glsl (GLSL's pow is implementation-defined: the harness routes it
+  to the oracle's refPow, the one pow both the oracle and the CUDA path use; textureGrad is a
+  stub that the tests never reach: their scenes carry no textures);
 
 applies mechanical GLSL-to-C++ rewrites (float literals stay single precision, swizzles become
 accessor calls, out / inout parameters references, int() / uint() of floats the GPU's saturating
@@ -46,6 +53,10 @@ SCANLINE_FUNCS = ["loadScanlineParamsRow", "loadScanlineParamsBin"]
 COUNTER_FUNCS = ["scanlineStep", "countSmallQuadBins", "loadScanlineParamsBin", "countLargeTriBins"]
 RASTER_FUNCS = ["rasterBinStep"]
 RASTER_LOW_FUNCS = ["scratchBlockRowOffset", "generateRowTris"]
+COLOR_FUNCS = ["decodeNormalUint", "decodeRGBA8", "encodeRGBA8", "linearToSRGB", "SRGBToLinear", "finalShading"]
+SHADING_FUNCS = ["getTriangleParams", "getTriangleVertexColors", "getTriangleVertexNormals",
+                 "getTriangleVertexTexCoords", "shadeSample"]
+REDUCE_FUNCS = ["initReduceSamples", "reduceSample", "finishReduceSamples"]
 
 
 def _read(*parts):
@@ -82,13 +93,15 @@ def _struct(text, name):
 
 
 FLOAT_LIT = re.compile(r"(?<![\w.])((?:\d+\.\d*|\.\d+)(?:[eE][-+]?\d+)?)(?![\w.])")
-SWIZZLE = re.compile(r"\.(xyz|xzw|xy|zw)\b(?!\s*\()")
+SWIZZLE = re.compile(r"\.(xyz|xzw|xy|zw|rgb)\b(?!\s*\()")
+COMPONENT = re.compile(r"\.([rgba])\b(?!\s*\()")
 OUT_PARAM = re.compile(r"\b(?:in\s+out|inout|out)\s+(\w+)\s+(\w+)")
 
 
 def _to_cpp(src):
     src = FLOAT_LIT.sub(r"\1f", src)      # GLSL float literals are single precision
     src = SWIZZLE.sub(r".\1()", src)       # swizzles: accessor calls of the shim's vector types
+    src = COMPONENT.sub(lambda m: "." + "xyzw"["rgba".index(m.group(1))], src)  # .r/.g/.b/.a
     src = OUT_PARAM.sub(r"\1& \2", src)    # out / inout parameters: references
     src = re.sub(r"\buvec4\(aabb\)", "toUvec4(aabb)", src)
     src = re.sub(r"\bint\(", "toInt(", src)    # int() / uint() of floats: the GPU's truncation
@@ -112,7 +125,7 @@ def generate():
     structs = _read("shared", "structures.glsl")
     out = ["// generated by oracle/ref_build.py from the reference's shader sources; not committed"]
     for line in defs.splitlines():
-        if re.match(r"#define\s+(INST_|REJECTION_TYPE_|STORAGE_)", line):
+        if re.match(r"#define\s+(INST_|REJECTION_TYPE_|STORAGE_|STATS_COUNT)", line):
             out.append(line)
     for line in setup.splitlines():
         if re.match(r"#define\s+(MAX_INSTANCE_QUADS|LSIZE|MAX_PACKET_SIZE)\b", line):
@@ -152,6 +165,27 @@ def generate():
         out.append(_to_cpp(_function(raster, name)))
     for name in RASTER_LOW_FUNCS:
         out.append(_to_cpp(_function(low, name)))
+    # shading and the 3-deep reduction window (shared/shading.glsl with shared/funcs.glsl)
+    shading = _read("shared", "shading.glsl")
+    for line in funcs.splitlines():
+        if re.match(r"#define\s+SATURATE\b", line):
+            out.append(line)
+    for m in re.finditer(r"^void swap\(inout (float|uint|int) a, inout \1 b\)", funcs, re.M):
+        out.append(_to_cpp(_block(funcs, m.start())))
+    for name in COLOR_FUNCS:
+        out.append(_to_cpp(_function(funcs, name)))
+    out.append("extern uint* g_instance_colors;\nextern vec4* g_instance_uv_rects;\n"
+               "extern sampler2D opaque_texture, transparent_texture;\nextern uint s_stats[STATS_COUNT];")
+    for name in SHADING_FUNCS:
+        out.append(_to_cpp(_function(shading, name)))
+    i0 = shading.index("#define RC_COLOR_SIZE")
+    i1 = shading.index("struct ReductionContext")
+    out.append(shading[i0:i1].strip())
+    out.append(_to_cpp(_struct(shading, "ReductionContext")))
+    m = re.search(r"^void swap\(inout ReductionContext", shading, re.M)
+    out.append(_to_cpp(_block(shading, m.start())))
+    for name in REDUCE_FUNCS:
+        out.append(_to_cpp(_function(shading, name)))
     return "\n\n".join(out) + "\n"
 
 

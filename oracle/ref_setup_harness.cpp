@@ -1,6 +1,6 @@
 /*
- * Harness of the reference's setup, bin-counter and row-span functions compiled as C++ (see
- * oracle/ref_build.py).
+ * Harness of the reference's setup, bin-counter, row-span, shading and reduction functions
+ * compiled as C++ (see oracle/ref_build.py).
  *
  * TEST INFRASTRUCTURE ONLY: tests/test_oracle_ref_pin.py compares its records with the oracle's
  * to pin the oracle's setup stage to the reference's own source. The functions that do the
@@ -21,6 +21,9 @@ namespace glsl {
 
 // specialization constants (definitions.glsl:40-58); the bin size is 32 in every build
 constexpr int BIN_SIZE = 32, BIN_SHIFT = 5;
+// one invocation at a time: a subgroup of one (shading.glsl's shuffles pick lane `bit`)
+#define SUBGROUP_SIZE 32
+#define HALFGROUP_SIZE 32
 int VIEWPORT_SIZE_X = 0, VIEWPORT_SIZE_Y = 0, MAX_VISIBLE_QUADS = 0, MAX_VISIBLE_TRIS = 0;
 int BIN_COUNT_X = 0, BIN_COUNT_Y = 0, BIN_COUNT = 0;
 struct {
@@ -42,6 +45,16 @@ uint* g_quad_aabbs;
 uvec4* g_uvec4_storage;
 uint* g_normals_storage;
 InstanceData* g_instances;
+uint* g_instance_colors;
+vec4* g_instance_uv_rects;
+sampler2D opaque_texture, transparent_texture;
+uint s_stats[STATS_COUNT];
+float (*g_pow)(float, float) = nullptr;
+int g_texture_calls = 0;
+
+// the last ref_quad_setup's storage, read by ref_shade_samples
+std::vector<uvec4> g_setup_storage;
+std::vector<uint> g_setup_normals;
 
 } // namespace glsl
 
@@ -95,8 +108,11 @@ int ref_quad_setup(const ref_setup_inputs* in, ref_setup_outputs* out) {
 	u_config.num_instances = in->num_instances;
 	u_config.instance_packet_size = c.instance_packet_size > 0 ? c.instance_packet_size : 1;
 
-	std::vector<uvec4> storage(size_t(mvq) * 14);
-	std::vector<uint> normals_storage(size_t(2) * mvq), quad_aabbs(mvq);
+	std::vector<uvec4>& storage = g_setup_storage;
+	std::vector<uint>& normals_storage = g_setup_normals;
+	storage.assign(size_t(mvq) * 14, uvec4());
+	normals_storage.assign(size_t(2) * mvq, 0u);
+	std::vector<uint> quad_aabbs(mvq);
 	std::vector<InstanceData> instances(size_t(in->num_instances));
 	std::memcpy(instances.data(), in->instances, sizeof(lucid_instance) * size_t(in->num_instances));
 	g_verts = const_cast<float*>(in->positions);
@@ -293,6 +309,55 @@ int ref_coverage(const uint32_t* quad_aabbs, const uint32_t* tri_scan, int32_t n
 			if(((quad_aabbs[q] >> (30 + second)) & 1u) == 0u)
 				tri(uint(q) * 2 + second, quad_aabbs[q]);
 	}
+	return 0;
+}
+
+// shadeSample (shading.glsl:107-184) of the samples (px[i], py[i], tris[i]) on the last
+// ref_quad_setup's records, with the scene's instance colours, lighting and background; RGBA8
+// colour and depth (inv_ray_pos) per sample. pow_fn is GLSL's implementation-defined pow.
+// Returns how many samples reached the texture stub (the tests' scenes have no textures: 0).
+int ref_shade_samples(const lucid_config* cfg, const uint32_t* instance_colors, float (*pow_fn)(float, float),
+					  int32_t n, const int32_t* px, const int32_t* py, const uint32_t* tris, uint32_t* colors,
+					  float* depths) {
+	g_uvec4_storage = g_setup_storage.data();
+	g_normals_storage = g_setup_normals.data();
+	g_instance_colors = const_cast<uint*>(instance_colors);
+	g_pow = pow_fn;
+	const lucid_lighting& L = cfg->lighting;
+	u_config.lighting.ambient_color = v4(L.ambient_color);
+	u_config.lighting.sun_color = v4(L.sun_color);
+	u_config.lighting.sun_dir = v4(L.sun_dir);
+	u_config.lighting.sun_power = L.sun_power;
+	u_config.lighting.ambient_power = L.ambient_power;
+	u_config.background_color = v4(cfg->background_color);
+	g_texture_calls = 0;
+	for(int i = 0; i < n; i++) {
+		float depth = 0.0f;
+		colors[i] = shadeSample(ivec2(px[i], py[i]), tris[i], depth);
+		depths[i] = depth;
+	}
+	return g_texture_calls;
+}
+
+// One pixel's samples (RGBA8 colour, depth) through the 3-deep reduction window:
+// initReduceSamples, reduceSample per sample, finishReduceSamples (shading.glsl:196-314). The
+// samples come in segments (seg[i], non-decreasing), as shadeAndReduceSamples hands them over
+// (raster.glsl:361-398): the colour a segment accumulates is saturated at its end.
+int ref_reduce(const float* background, int32_t n, const uint32_t* colors, const float* depths, const int32_t* seg,
+			   float* rgba) {
+	u_config.background_color = v4(background);
+	ReductionContext ctx;
+	initReduceSamples(ctx);
+	for(int i = 0; i < n;) {
+		vec3 out_color = ctx.out_color;
+		const int sg = seg[i];
+		for(; i < n && seg[i] == sg; i++)
+			reduceSample(ctx, out_color, uvec2(colors[i], floatBitsToUint(depths[i])), 1u);
+		ctx.out_color = SATURATE(out_color);
+	}
+	const vec4 r = finishReduceSamples(ctx);
+	for(int k = 0; k < 4; k++)
+		rgba[k] = r[k];
 	return 0;
 }
 
