@@ -508,6 +508,86 @@ __device__ __forceinline__ void forEachGroupFragment(const FrameParams& p, const
 	}
 }
 
+// forEachGroupFragment's four-entry mode with the row's relevant entries staged in shared memory:
+// a warp compacts the entries of its slice that take part (span in the group's columns, key range
+// meeting [flo, fhi] when `ekeys` is given) into its kStageEntries-entry area of `stage`, up to
+// kStageEntries at a time, then every lane reads them four per step with broadcast loads (one
+// 16-byte load per entry instead of four shuffles). fn(t, on[4], key[4], tri[4]).
+constexpr int kStageEntries = 256;
+static_assert(NW * kStageEntries * 16 <= 2 * kGroupCap * 4, "the staged entries live in one sort buffer");
+template <typename Fn>
+__device__ __forceinline__ void forEachGroupFragmentStaged(const FrameParams& p, const RasterSmem& s,
+														   const uint2* scratch, const float4* planes, int band_cap,
+														   int bin_x, int bin_y, int p0, int p1, Fn fn, uint4* stage,
+														   const uint2* ekeys, uint32_t flo, uint32_t fhi) {
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	const int r0 = p0 >> 5, r1 = (p1 - 1) >> 5;
+	const int nrows = r1 - r0 + 1;
+	const int per_row = NW / nrows;
+	if(warp >= per_row * nrows)
+		return;
+	const int row = r0 + warp / per_row, slice = warp % per_row;
+	const int b = row >> 2, rshift = 5 * (row & 3);
+	const int ne = s.band_count[b];
+	const int jbeg = int((int64_t(ne) * slice) / per_row), jend = int((int64_t(ne) * (slice + 1)) / per_row);
+	const int pix = row * 32 + lane;
+	const bool in_group = pix >= p0 && pix < p1;
+	const int t = pix - p0;
+	const float fx = float(bin_x + lane), fy = float(bin_y + row);
+	const int glo = max(0, p0 - 32 * row), ghi = min(31, p1 - 1 - 32 * row);
+	const uint32_t lt = laneMaskLt();
+	uint4* ws = stage + warp * kStageEntries;
+	const size_t bbase = size_t(b) * band_cap;
+	uint2 n_e = make_uint2(0u, 0u), n_kr = make_uint2(0u, 0xffffffffu);
+	float4 n_d = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+	if(jbeg + lane < jend) {
+		n_e = scratch[bbase + jbeg + lane];
+		n_d = planes[bbase + jbeg + lane];
+		if(ekeys)
+			n_kr = ekeys[bbase + jbeg + lane];
+	}
+	for(int s0 = jbeg; s0 < jend; s0 += kStageEntries) {
+		const int s1 = min(s0 + kStageEntries, jend);
+		int n = 0;
+		for(int j0 = s0; j0 < s1; j0 += 32) {
+			const int j = j0 + lane;
+			bool rel = j < s1;
+			const uint2 e = n_e, kr = n_kr;
+			const float4 d = n_d;
+			if(j + 32 < jend) {
+				n_e = scratch[bbase + j + 32];
+				n_d = planes[bbase + j + 32];
+				if(ekeys)
+					n_kr = ekeys[bbase + j + 32];
+			}
+			if(rel && ekeys)
+				rel = kr.y >= flo && kr.x <= fhi;
+			const int lo = (e.x >> rshift) & 31, hi = (e.y >> rshift) & 31;
+			rel = rel && max(lo, glo) <= min(hi, ghi);
+			const uint32_t m = __ballot_sync(0xffffffffu, rel);
+			if(rel)
+				ws[n + __popc(m & lt)] = make_uint4(uint32_t(lo) | uint32_t(hi) << 5, entryTri(e),
+													__float_as_uint(d.x), __float_as_uint(d.y * fy + d.z));
+			n += __popc(m);
+		}
+		__syncwarp();
+		for(int i = 0; i < n; i += 4) {
+			bool on[4];
+			uint32_t key[4], tr[4];
+#pragma unroll
+			for(int u = 0; u < 4; u++) {
+				const bool has = i + u < n;
+				const uint4 q = ws[has ? i + u : i];
+				key[u] = nearFirstKey(__uint_as_float(q.z) * fx + __uint_as_float(q.w));
+				tr[u] = q.y;
+				on[u] = has && in_group && lane >= int(q.x & 31u) && lane <= int(q.x >> 5);
+			}
+			fn(t, on, key, tr);
+		}
+		__syncwarp();
+	}
+}
+
 // Input primitive id of a tri slot (ties between equal depth keys go by it).
 __device__ __forceinline__ uint32_t triPrim(const FrameParams& p, uint32_t tri) {
 	return __ldg(p.quad_source + (tri >> 1)) * 2 + (tri & 1);
@@ -1366,22 +1446,24 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 #if LUCID_RASTER_COUNTERS
 				const long long tw0 = clock64();
 #endif
-				constexpr int AU = 4; // entries per step (8 measured slower)
-				forEachGroupFragment<true, AU>(p, s, scratch, planes, band_cap, bin_x, bin_y, p0, p1,
-										   [&](int tp, const bool* on, const uint32_t* key, const uint32_t* tri) {
-											   const int end = (tp + 1) * rcap;
-											   int pos[AU];
+				constexpr int AU = 4; // entries per step (8 measured slower than 4)
+				auto append = [&](int tp, const bool* on, const uint32_t* key, const uint32_t* tri) {
+					const int end = (tp + 1) * rcap;
+					int pos[AU];
 #pragma unroll
-											   for(int u = 0; u < AU; u++)
-												   pos[u] = on[u] && key[u] >= lo_k && key[u] <= hi_k ? atomicAdd(&s.px_wend[tp], 1) : end;
+					for(int u = 0; u < AU; u++)
+						pos[u] = on[u] && key[u] >= lo_k && key[u] <= hi_k ? atomicAdd(&s.px_wend[tp], 1) : end;
 #pragma unroll
-											   for(int u = 0; u < AU; u++)
-												   if(pos[u] < end) {
-													   s.kv[1][0][pos[u]] = key[u];
-													   s.kv[1][1][pos[u]] = fragPayload(tp, tri[u]);
-												   }
-										   },
-										   cull ? ekeys : nullptr, 0u, 0, cull ? lo_k : 1u, cull ? hi_k : 0u);
+					for(int u = 0; u < AU; u++)
+						if(pos[u] < end) {
+							s.kv[1][0][pos[u]] = key[u];
+							s.kv[1][1][pos[u]] = fragPayload(tp, tri[u]);
+						}
+				};
+				// the idle window buffer holds the warps' staged entries
+				forEachGroupFragmentStaged(p, s, scratch, planes, band_cap, bin_x, bin_y, p0, p1, append,
+										   reinterpret_cast<uint4*>(&s.kv[0][0][0]), cull ? ekeys : nullptr,
+										   cull ? lo_k : 0u, cull ? hi_k : 0xffffffffu);
 #if LUCID_RASTER_COUNTERS
 				if(lane == 0)
 					rc[16] += clock64() - tw0;
