@@ -740,10 +740,27 @@ __device__ unsigned long long lightRow(const FrameParams& p, const RasterSmem& s
 						// full: the new fragment replaces the farthest one kept
 						K[off + maxi] = key;
 						V[off + maxi] = t;
-						maxi = 0, maxk = K[off], maxt = V[off];
-						for(int i = 1; i < cap; i++)
-							if(fragBefore(p, maxk, maxt, K[off + i], V[off + i]))
-								maxi = i, maxk = K[off + i], maxt = V[off + i];
+						// the farthest kept fragment: the largest key without a branch per element,
+						// equal keys (rare) by the larger input primitive id in a second scan
+						maxi = 0, maxk = K[off];
+						bool tie = false;
+						for(int i = 1; i < cap; i++) {
+							const uint32_t ki = K[off + i];
+							const bool gt = ki > maxk;
+							tie = gt ? false : (tie || ki == maxk);
+							maxi = gt ? i : maxi;
+							maxk = gt ? ki : maxk;
+						}
+						maxt = V[off + maxi];
+						if(tie) {
+							uint32_t bp = triPrim(p, maxt);
+							for(int i = 0; i < cap; i++)
+								if(K[off + i] == maxk && i != maxi) {
+									const uint32_t pi = triPrim(p, V[off + i]);
+									if(pi > bp)
+										maxi = i, bp = pi, maxt = V[off + i];
+								}
+						}
 					}
 				}
 			}
@@ -764,10 +781,24 @@ __device__ unsigned long long lightRow(const FrameParams& p, const RasterSmem& s
 		auto take = [&](uint32_t& key, uint32_t& tri) {
 			int bi = off;
 			key = K[off];
+			// the nearest key without a branch per element; equal keys (rare) are then ordered by
+			// input primitive id in a second scan
+			bool tie = false;
 			for(int i = off + 1; i < off + n; i++) {
 				const uint32_t ki = K[i];
-				if(ki < key || (ki == key && triPrim(p, V[i]) < triPrim(p, V[bi])))
-					bi = i, key = ki;
+				const bool lt = ki < key;
+				tie = lt ? false : (tie || ki == key);
+				bi = lt ? i : bi;
+				key = lt ? ki : key;
+			}
+			if(tie) {
+				uint32_t bp = triPrim(p, V[bi]);
+				for(int i = off; i < off + n; i++)
+					if(K[i] == key && i != bi) {
+						const uint32_t pi = triPrim(p, V[i]);
+						if(pi < bp)
+							bi = i, bp = pi;
+					}
 			}
 			tri = V[bi];
 			K[bi] = K[off + n - 1];
