@@ -293,3 +293,25 @@ def test_largest_viewport(gpu, oracle):
                             large_fraction=0.02, large_area=(50000.0, 100000.0))
     g, o = compare(sc, oracle, image64=False)
     assert o["bin_count"] == 16384 and o["num_visible"][1] > 0
+
+
+@pytest.mark.parametrize("copies", [6, 40, 90])
+def test_exact_depth_ties(gpu, oracle, copies):
+    """Every triangle drawn several times over (identical vertices, other colours): equal depth
+    keys at every pixel, ordered by input primitive id. 6 copies stay in the light path's
+    single pass, 40 need its bounded passes (more than 32 fragments per pixel), 90 take the
+    depth windows (more than 64)."""
+    rng = np.random.default_rng(100 + copies)
+    tris, cols = [], []
+    for _ in range(12):
+        x0, y0 = rng.uniform(-10, 60, 2)
+        d = rng.uniform(1.0, 50.0, 3)
+        base = [(x0, y0, d[0]), (x0 + rng.uniform(20, 60), y0 + rng.uniform(-5, 10), d[1]),
+                (x0 + rng.uniform(-5, 10), y0 + rng.uniform(20, 50), d[2])]
+        for _ in range(copies):
+            tris.append(base)
+            cols.append([(int(c[0]), int(c[1]), int(c[2]), 30) for c in rng.integers(0, 255, (3, 3))])
+    order = rng.permutation(len(tris))  # copies of one triangle spread over the input order
+    sc = scenes.screen_triangles([tris[i] for i in order], [cols[i] for i in order], 96, 72)
+    g, o = compare(sc, oracle, dump=128)
+    assert o["max_pixel_fragments"] >= copies
