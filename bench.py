@@ -260,6 +260,7 @@ def run_reference(args, rank):
     bins = args.cpu_sample_bins or 48
     cores = host_cores()
     vals = []
+    times = []
     last = None
     for i in range(args.warmup + args.steps):
         r = cpu_sample(scene, bins, cores, seed=i)
@@ -269,13 +270,15 @@ def run_reference(args, rank):
         frame_time = r["t_bin"] + frame_frags / rate
         if i >= args.warmup:
             vals.append(frame_frags / frame_time)
+            times.append(frame_time)
         last = r
     value = float(np.mean(vals))
+    ms_per_step = float(np.mean(times)) * 1e3
     sample = (f"setup+binning of the full scene, raster of {last['bins']} seeded random bins "
               f"of {last['bin_count']} per step; frame time extrapolated by fragments")
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": workload_config(args.workload, scene), "impl": "reference",
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": sample},
