@@ -1441,11 +1441,11 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 				rc[14] += clock64() - tc2;
 #endif
 			// Direct slab 0: one pass over the band entries appends every fragment of the slab to
-			// its pixel's region of the idle sort buffer (kGroupCap / npix fragments per pixel);
-			// the per-pixel bucket counts are then taken from the regions in shared memory, and
-			// the first window is scattered from them instead of generated from the entries
-			// again. A pixel whose slab overflows its region sends the group to the histogram
-			// pass over the entries.
+			// its pixel's region of the idle sort buffer (kGroupCap / npix fragments per pixel)
+			// and counts it in its pixel's bucket, and the first window is scattered from the
+			// regions instead of generated from the entries again. A pixel whose slab overflows
+			// its region sends the group to the histogram pass over the entries (which counts
+			// the buckets afresh).
 			// odd region stride: the pixels of a row append at similar cursors, so that their
 			// stores fall into different banks
 			const int rcap = ((kGroupCap / max(npix, 1)) - 1) | 1;
@@ -1467,12 +1467,15 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 				}
 				if(t < npix)
 					s.px_wend[t] = t * rcap;
+				for(int i = tid; i < (npix << nb_log); i += RT)
+					s.hist[i] = 0;
 				__syncthreads();
 				slab_lo = s.slab_lo, slab_hi = s.slab_hi;
 				const uint32_t range = slab_hi - slab_lo;
 				const int bits = range ? 32 - __clz(range) : 0;
 				shift = max(0, bits - nb_log);
 				const uint32_t lo_k = slab_lo, hi_k = slab_hi;
+				const int sh = shift;
 				const bool cull = lo_k > s.kmin || hi_k < s.kmax;
 #if LUCID_RASTER_COUNTERS
 				const long long tw0 = clock64();
@@ -1489,6 +1492,7 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 						if(pos[u] < end) {
 							s.kv[1][0][pos[u]] = key[u];
 							s.kv[1][1][pos[u]] = fragPayload(tp, tri[u]);
+							atomicAdd(&s.hist[histIdx(tp, int((key[u] - lo_k) >> sh), nb_log)], 1u);
 						}
 				};
 				// the idle window buffer holds the warps' staged entries
@@ -1510,16 +1514,6 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 				}
 				if(t < npix)
 					s.px_rend[t] = s.px_wend[t] - t * rcap;
-				for(int i = tid; i < (npix << nb_log); i += RT)
-					s.hist[i] = 0;
-				__syncthreads();
-				const int sh = shift;
-				for(int tp = warp; tp < npix; tp += NW) {
-					const int beg = tp * rcap, n = s.px_rend[tp];
-					for(int k = lane; k < n; k += 32)
-						atomicAdd(&s.hist[histIdx(tp, int((s.kv[1][0][beg + k] - lo_k) >> sh), nb_log)], 1u);
-				}
-				__syncthreads();
 				if(t < npix && s.px_state[t] != 1) {
 					s.px_state[t] = 0;
 					s.px_lo[t] = 0;
