@@ -371,6 +371,12 @@ __device__ void writePixel(const FrameParams& p, int px, int py, float4 c) {
 		reinterpret_cast<float4*>(p.out_rgba)[size_t(py) * p.width + px] = c;
 }
 
+// ne * k / d for 0 <= k <= d <= 16 (a warp's slice of a band's entries) in 32-bit arithmetic
+// while ne * k fits, instead of a 64-bit division
+__device__ __forceinline__ int sliceBound(int ne, int k, int d) {
+	return ne < (1 << 28) ? int((uint32_t(ne) * uint32_t(k)) / uint32_t(d)) : int((int64_t(ne) * k) / d);
+}
+
 // Visits every fragment of pixels [p0, p1) of the bin: fn(t, key, tri) with t the pixel
 // index inside the group, called by the lane owning pixel t. Warps are assigned to the group's
 // rows (lane = pixel column) and split a row's band entries; entries are loaded 32 at a time
@@ -397,7 +403,7 @@ __device__ __forceinline__ void forEachGroupFragment(const FrameParams& p, const
 	const int row = r0 + warp / per_row, slice = warp % per_row;
 	const int b = row >> 2, rshift = 5 * (row & 3);
 	const int ne = s.band_count[b];
-	const int jbeg = int((int64_t(ne) * slice) / per_row), jend = int((int64_t(ne) * (slice + 1)) / per_row);
+	const int jbeg = sliceBound(ne, slice, per_row), jend = sliceBound(ne, slice + 1, per_row);
 	const int pix = row * 32 + lane;
 	const bool in_group = pix >= p0 && pix < p1;
 	const int t = pix - p0;
@@ -529,7 +535,7 @@ __device__ __forceinline__ void forEachGroupFragmentStaged(const FrameParams& p,
 	const int row = r0 + warp / per_row, slice = warp % per_row;
 	const int b = row >> 2, rshift = 5 * (row & 3);
 	const int ne = s.band_count[b];
-	const int jbeg = int((int64_t(ne) * slice) / per_row), jend = int((int64_t(ne) * (slice + 1)) / per_row);
+	const int jbeg = sliceBound(ne, slice, per_row), jend = sliceBound(ne, slice + 1, per_row);
 	const int pix = row * 32 + lane;
 	const bool in_group = pix >= p0 && pix < p1;
 	const int t = pix - p0;
