@@ -1679,7 +1679,7 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 								const int c = cntq[q][k];
 								if(k <= lastk[q] && c >= 2) {
 									if(c <= 16)
-										ccount += 1ull << (16 * (c <= 2 ? 0 : c <= 4 ? 1 : c <= 8 ? 2 : 3));
+										ccount += 1ull << (16 * (31 - __clz(c - 1)));
 									else if(c <= 256)
 										lcount++;
 									else
@@ -1703,7 +1703,9 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 						}
 						cbase = __shfl_sync(0xffffffffu, cbase, 31);
 						lbase = __shfl_sync(0xffffffffu, lbase, 31);
-						unsigned long long cpos = cbase + cincl - ccount; // this lane's first slot per class
+						const unsigned long long cpos = cbase + cincl - ccount; // this lane's first slot per class
+						// the slots of classes 0-1 and 2-3, 16 bits each (no field carries into the next)
+						uint32_t cp01 = uint32_t(cpos), cp23 = uint32_t(cpos >> 32);
 						int lpos = lbase + lincl - lcount;
 #pragma unroll
 						for(int q = 0; q < 2; q++) {
@@ -1716,20 +1718,20 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 									if(bk >= lo[q]) {
 										s.hist[histIdx(tpq[q], bk, nb_log)] = uint32_t(rel);
 										if(c >= 2 && c <= 16) {
-											const int cls = c <= 2 ? 0 : c <= 4 ? 1 : c <= 8 ? 2 : 3;
-											const int pos = int((cpos >> (16 * cls)) & 0xffffull);
-											cpos += 1ull << (16 * cls);
+											const int cls = 31 - __clz(c - 1); // 2 -> 0, 3-4 -> 1, 5-8 -> 2, 9-16 -> 3
+											const bool back = cls >= 2;        // classes 2 and 3 fill their lists from the back
+											const uint32_t sh16 = uint32_t(cls & 1) << 4;
+											const int pos = int(((back ? cp23 : cp01) >> sh16) & 0xffffu);
+											cp01 += back ? 0u : 1u << sh16;
+											cp23 += back ? 1u << sh16 : 0u;
 											const uint32_t entry = segEntry(rel, c, tpq[q]);
-											if(pos >= kList) // lists overflow: the window is radix sorted
-												;
-											else if(cls == 0)
-												s.sub_small[pos] = entry;
-											else if(cls == 1)
-												s.radix[pos] = entry;
-											else if(cls == 2)
-												s.sub_small[kList - 1 - pos] = entry;
-											else
-												s.radix[kList - 1 - pos] = entry;
+											const int idx = back ? kList - 1 - pos : pos;
+											if(pos < kList) { // lists overflow: the window is radix sorted
+												if(cls & 1)
+													s.radix[idx] = entry;
+												else
+													s.sub_small[idx] = entry;
+											}
 										} else if(c > 16 && c <= 256) {
 											if(lpos < kGroupCap / 17 + 1)
 												s.sub_large[lpos] = segEntry(rel, c, tpq[q]);
