@@ -2032,10 +2032,16 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 				uint32_t* K = s.kv[cur][0];
 				uint32_t* V = s.kv[cur][1];
 
-				// C5. equal-depth runs in primitive order
+				// C5. equal-depth runs in primitive order (a run starts where the next fragment has
+				// the same key and pixel and the previous one does not; equal neighbouring keys are
+				// rare, so most elements read two keys and nothing else)
 				for(int i = tid; i < n; i += RT) {
-					bool same_prev = i > 0 && K[i - 1] == K[i] && ((V[i - 1] ^ V[i]) & 0xffu) == 0;
-					bool same_next = i + 1 < n && K[i + 1] == K[i] && ((V[i + 1] ^ V[i]) & 0xffu) == 0;
+					const uint32_t ki = K[i];
+					if(i + 1 >= n || K[i + 1] != ki)
+						continue;
+					const uint32_t vi = V[i];
+					const bool same_prev = i > 0 && K[i - 1] == ki && ((V[i - 1] ^ vi) & 0xffu) == 0;
+					const bool same_next = ((V[i + 1] ^ vi) & 0xffu) == 0;
 					if(!same_prev && same_next) {
 						int e = i + 1;
 						while(e < n && K[e] == K[i] && ((V[e] ^ V[i]) & 0xffu) == 0)
