@@ -103,6 +103,7 @@ struct RasterSmem {
 	int px_done[kGroupPixels];   // fragments already processed (verification dump index)
 	int px_state[kGroupPixels];  // 0 active, 1 finished
 	int px_rend[kGroupPixels];   // fragments of the pixel's region of a directly generated slab
+	int px_slot[kGroupPixels];   // shading round: blend cursor | fragments to shade << 16
 	// sub-segments of the current window that need sorting, as (start << 16 | count):
 	// counts 2..16 are sorted by one thread, by size class (2, 3-4, 5-8, 9-16; class 0 from the
 	// front and class 2 from the back of sub_small, classes 1 and 3 likewise in `radix`, which
@@ -2089,6 +2090,14 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 					// start in different shared-memory banks
 					const int batch = (min(round == 0 ? kShadeFirst : kShadeNext, kStage / max(npix, 1)) - 1) | 1;
 					if constexpr(MODE != kRasterBackward) {
+						// per pixel: the blend cursor (< kGroupCap) and the fragments to shade in
+						// this round (<= batch), read by every slot of the pixel with one load
+						if(t < npix) {
+							const int b = s.px_bcur[t];
+							const int m = s.px_state[t] == 0 ? max(0, min(batch, s.px_wend[t] - b)) : 0;
+							s.px_slot[t] = b | (m << 16);
+						}
+						__syncthreads();
 						// slot / batch by multiply and shift (exact for odd batch in [15, 255] and
 						// slot < 4096)
 						const uint32_t bmul = (1u << 20) / uint32_t(batch) + 1u;
@@ -2103,9 +2112,10 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 							for(int q = 0; q < 2; q++) {
 								const int slot = slot0 + q * RT;
 								tq[q] = int((uint32_t(slot) * bmul) >> 20);
-								const int tpc = min(tq[q], npix - 1);
-								fq[q] = s.px_bcur[tpc] + (slot - tq[q] * batch);
-								okq[q] = slot < nslots && fq[q] < s.px_wend[tpc] && s.px_state[tpc] == 0;
+								const int ps = s.px_slot[min(tq[q], npix - 1)];
+								const int j = slot - tq[q] * batch;
+								fq[q] = (ps & 0xffff) + j;
+								okq[q] = slot < nslots && j < (ps >> 16);
 								vq[q] = okq[q] ? V[fq[q]] : 0u;
 								kq[q] = okq[q] ? K[fq[q]] : 0u;
 							}
