@@ -1312,15 +1312,11 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 						float dx = d.x, dy = d.y, dz = d.z;
 						uint32_t emn = 0xffffffffu, emx = 0u;
 						int wsum = 0;
-#pragma unroll
-						for(int r = 0; r < 4; r++) {
-							int row = b * 4 + r;
-							if(row < r0 || row > r1)
-								continue;
+						auto rowRange = [&](int r, int row) {
 							int lo = (e.x >> (5 * r)) & 31, hi = (e.y >> (5 * r)) & 31;
 							int xlo = max(lo, p0 - 32 * row), xhi = min(hi, p1 - 1 - 32 * row);
 							if(xlo > xhi)
-								continue;
+								return;
 							wsum += xhi - xlo + 1;
 							// the evaluation is monotone in x, so the row's extremes are its ends
 							float ty = dy * float(bin_y + row) + dz;
@@ -1328,6 +1324,16 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 							uint32_t kb = nearFirstKey(dx * float(bin_x + xhi) + ty);
 							emn = min(emn, min(ka, kb));
 							emx = max(emx, max(ka, kb));
+						};
+						if(r0 == r1) { // a one-row group (the common case): its band's row only
+							rowRange(r0 & 3, r0);
+						} else {
+#pragma unroll
+							for(int r = 0; r < 4; r++) {
+								int row = b * 4 + r;
+								if(row >= r0 && row <= r1)
+									rowRange(r, row);
+							}
 						}
 						kmn = min(kmn, emn);
 						kmx = max(kmx, emx);
