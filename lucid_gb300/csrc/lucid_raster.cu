@@ -1516,7 +1516,7 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 				if(lane == 0)
 					rc[16] += clock64() - tw0;
 #endif
-				__syncthreads();
+				__syncthreads(); // every append is done before a pixel's cursor is tested below
 #if LUCID_RASTER_COUNTERS
 				if(tid == 0)
 					rc[17] += clock64() - tw0;
@@ -1963,7 +1963,8 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 								   uint32_t(filled - s.px_wbase[t]));
 					s.px_wend[t] = want;
 				}
-				__syncthreads();
+				// no barrier: the sorts below read neither px_wend nor the cursors, and thread t
+				// alone reads px_wend[t] until the next barrier
 #if LUCID_RASTER_COUNTERS
 				if(tid == 0)
 					rc[13] += clock64() - tc2;
@@ -2017,9 +2018,10 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 					}
 				}
 				__syncthreads();
-				if(tid == 0) // the lists are consumed: the next window's start empty
+				// the lists are consumed: the next window's start empty (read again only by the next
+				// window's selection, after further barriers)
+				if(tid == 0)
 					s.n_cls = 0ull, s.n_large = 0;
-				__syncthreads();
 				RASTER_TIMER(4);
 				const bool use_radix = any_big && n > 1;
 				if(tid == 0) {
