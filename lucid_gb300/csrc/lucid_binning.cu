@@ -396,7 +396,7 @@ __device__ __forceinline__ uint32_t refKey(uint32_t v) { return v & 0x0fffffffu;
 // each merge pairs i with its mirror in the k-block, the later ones with i ^ j.
 __device__ __forceinline__ int bitonicPartner(int i, int k, int j) { return j == (k >> 1) ? i ^ (k - 1) : i ^ j; }
 
-template <class Src> __global__ void __launch_bounds__(kSortThreads) binSortKernel(Src src) {
+template <class Src> __global__ void __launch_bounds__(kSortThreads, 4) binSortKernel(Src src) {
 	__shared__ uint32_t s_v[kSortCap];
 	int cta, ncta;
 	const FrameParams& p = src.get(cta, ncta);
