@@ -21,8 +21,8 @@
 //     covers about slab_target fragments per unfinished pixel (from an estimate gathered with
 //     the group's key range); the next slab is counted only if a pixel needs it. The first
 //     slab is generated directly: one pass over the band entries appends its fragments to
-//     per-pixel regions of the idle sort buffer, the histograms are counted from there, and the
-//     first window is scattered from the regions (no second pass over the entries).
+//     per-pixel regions of the idle sort buffer and counts each in its pixel's histogram, and
+//     the first window is scattered from the regions (no second pass over the entries).
 //  D. Per window: fragments (32-bit nearest-first depth key, 32-bit payload = pixel | tri) are
 //     generated by one warp per pixel row (lane = pixel, band entries broadcast by shuffle) and
 //     written to their pixel's segment, in a heavy group to the sub-segment of their depth
