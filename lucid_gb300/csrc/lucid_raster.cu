@@ -1657,7 +1657,9 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 							excl[q] = incl[q] - lsum[q];
 						}
 						// per lane: included buckets (k <= lastk) and the packed class counts
-						unsigned long long ccount = 0ull;
+						// this lane's sub-segments per size class, 16 bits each: classes 0-1 and 2-3
+						// (no field carries into the next)
+						uint32_t cc01 = 0u, cc23 = 0u;
 						int lcount = 0, lastk[2];
 #pragma unroll
 						for(int q = 0; q < 2; q++) {
@@ -1685,34 +1687,37 @@ __global__ void __launch_bounds__(RT, 1) rasterKernel(Work work) {
 							for(int k = 0; k < 4; k++) {
 								const int c = cntq[q][k];
 								if(k <= lastk[q] && c >= 2) {
-									if(c <= 16)
-										ccount += 1ull << (16 * (31 - __clz(c - 1)));
-									else if(c <= 256)
+									if(c <= 16) {
+										const int cls = 31 - __clz(c - 1);
+										const uint32_t inc = 1u << ((cls & 1) << 4);
+										cc01 += cls < 2 ? inc : 0u;
+										cc23 += cls < 2 ? 0u : inc;
+									} else if(c <= 256)
 										lcount++;
 									else
 										big = true;
 								}
 							}
 						}
-						const unsigned long long cincl = warpInclusiveScan(ccount);
+						const uint32_t ci01 = warpInclusiveScan(cc01), ci23 = warpInclusiveScan(cc23);
 						const int lincl = warpInclusiveScan(lcount);
-						unsigned long long cbase = 0ull;
+						uint32_t b01 = 0u, b23 = 0u;
 						int lbase = 0;
 						if(lane == 31) {
-							if(cincl)
-							{
-								uint32_t* nc32 = reinterpret_cast<uint32_t*>(&s.n_cls);
-								const uint32_t b0 = atomicAdd(nc32, uint32_t(cincl)), b1 = atomicAdd(nc32 + 1, uint32_t(cincl >> 32));
-								cbase = (unsigned long long)b0 | ((unsigned long long)b1 << 32);
-							}
+							// the two 32-bit halves of the packed class counts
+							uint32_t* nc32 = reinterpret_cast<uint32_t*>(&s.n_cls);
+							if(ci01)
+								b01 = atomicAdd(nc32, ci01);
+							if(ci23)
+								b23 = atomicAdd(nc32 + 1, ci23);
 							if(lincl)
 								lbase = atomicAdd(&s.n_large, lincl);
 						}
-						cbase = __shfl_sync(0xffffffffu, cbase, 31);
+						b01 = __shfl_sync(0xffffffffu, b01, 31);
+						b23 = __shfl_sync(0xffffffffu, b23, 31);
 						lbase = __shfl_sync(0xffffffffu, lbase, 31);
-						const unsigned long long cpos = cbase + cincl - ccount; // this lane's first slot per class
-						// the slots of classes 0-1 and 2-3, 16 bits each (no field carries into the next)
-						uint32_t cp01 = uint32_t(cpos), cp23 = uint32_t(cpos >> 32);
+						// this lane's first slot per class
+						uint32_t cp01 = b01 + ci01 - cc01, cp23 = b23 + ci23 - cc23;
 						int lpos = lbase + lincl - lcount;
 #pragma unroll
 						for(int q = 0; q < 2; q++) {
